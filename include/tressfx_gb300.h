@@ -1,0 +1,256 @@
+/*
+ * tressfx_gb300.h -- C ABI of the GB300 (sm_103a) TressFX strand-simulation + SDF-collision library.
+ *
+ * The reference drives its HLSL compute shaders through the Engine Interface (EI):
+ * EI_Device::CreateBufferResource / CreateComputeShaderPSO / CreateBindSet and
+ * EI_CommandContext::BindPSO / BindSets / Dispatch / UpdateBuffer / SubmitBarrier
+ * (src/EngineInterface.h:23-31, src/DX12/DX12EngineInterfaceImpl.cpp:1000-1014, 1600, 1638-1650).
+ * This header is the replacement for that compute path: plain pointers, sizes and opaque handles,
+ * every call returns an int status (0 = TFX_OK), nothing throws across it, and all device work is
+ * issued in order on the CUDA stream owned by a tfx_context (the EI_CommandContext).
+ *
+ * Layout conventions (identical to the reference buffers, TressFXHairObject.cpp:60-105):
+ *   - vertex buffers are float4 (16 B), strand-major: vertex j of strand s sits at s*n + j;
+ *   - follow strands follow their guide: guide g is strand g*(F+1), its follows g*(F+1)+1..+F;
+ *   - position.w is the inverse mass, w <= 0 marks an immovable vertex;
+ *   - bone matrices are 16 floats, row-major, row-vector convention (p' = [p 1] * M), as the
+ *     shader's `row_major float4x4 g_BoneSkinningMatrix[]` reads them (TressFXSimulation.hlsl:70).
+ */
+#ifndef TRESSFX_GB300_H_
+#define TRESSFX_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TFX_ABI_VERSION 1
+#define TFX_MAX_BONES 512              /* AMD_TRESSFX_MAX_NUM_BONES, src/TressFX/AMD_TressFX.h:45-47 */
+#define TFX_THREAD_GROUP_SIZE 64       /* TRESSFX_SIM_THREAD_GROUP_SIZE, src/TressFX/TressFXCommon.h:34 */
+
+/* ---------------------------------------------------------------------------------- status */
+typedef enum tfx_status {
+    TFX_OK = 0,
+    TFX_ERR_INVALID_ARGUMENT = 1,   /* null handle/pointer, negative count, unknown id          */
+    TFX_ERR_VERTS_PER_STRAND = 2,   /* n not in {4, 8, 16, 32, 64} (TressFXAsset.cpp:115-118)    */
+    TFX_ERR_BONE_INDEX = 3,         /* a skinning bone index outside [0, 512)                    */
+    TFX_ERR_BONE_WEIGHTS = 4,       /* skinning weights whose shader-side sum is <= 0            */
+    TFX_ERR_CUDA = 5,               /* a CUDA runtime call or kernel launch failed               */
+    TFX_ERR_OUT_OF_MEMORY = 6,
+    TFX_ERR_TIMEOUT = 7,            /* a bounded device-side wait gave up                        */
+    TFX_ERR_SIZE = 8,               /* counts that overflow the 32-bit vertex index space        */
+    TFX_ERR_MISMATCH = 9,           /* constants whose counts disagree with the object           */
+    TFX_ERR_NO_DEVICE = 10          /* no CUDA device, or not an sm_103 device                   */
+} tfx_status;
+
+/* Human-readable name of a status code. */
+const char* tfx_status_string(int status);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* tfx_last_error(void);
+/* TFX_ABI_VERSION of the loaded library. */
+int tfx_abi_version(void);
+
+/* ---------------------------------------------------------------------------------- handles */
+typedef struct tfx_context_t* tfx_context;   /* EI_CommandContext: one CUDA stream            */
+typedef struct tfx_hair_t* tfx_hair;         /* TressFXHairObject + TressFXDynamicState       */
+typedef struct tfx_sdf_t* tfx_sdf;           /* TressFXSDFCollision's signed distance grid    */
+typedef struct tfx_mesh_t* tfx_mesh;         /* TressFXBoneSkinning's skinned collision mesh  */
+
+/* Kernel ids: one per reference compute entry point. */
+typedef enum tfx_kernel {
+    TFX_KERNEL_INTEGRATION_AND_GLOBAL_SHAPE = 1, /* IntegrationAndGlobalShapeConstraints, TressFXSimulation.hlsl:609-666 */
+    TFX_KERNEL_STRAND_LEVEL_DATA = 2,            /* CalculateStrandLevelData,             TressFXSimulation.hlsl:677-728 */
+    TFX_KERNEL_VELOCITY_SHOCK_PROPAGATION = 3,   /* VelocityShockPropagation,             TressFXSimulation.hlsl:739-762 */
+    TFX_KERNEL_LOCAL_SHAPE_CONSTRAINTS = 4,      /* LocalShapeConstraints,                TressFXSimulation.hlsl:773-829 */
+    TFX_KERNEL_LENGTH_WIND_COLLISION = 5,        /* LengthConstriantsWindAndCollision,    TressFXSimulation.hlsl:875-975 */
+    TFX_KERNEL_UPDATE_FOLLOW_HAIR = 6,           /* UpdateFollowHairVertices,             TressFXSimulation.hlsl:978-1001 */
+    TFX_KERNEL_SDF_INITIALIZE = 7,               /* InitializeSignedDistanceField,        TressFXSDFCollision.hlsl:301-312 */
+    TFX_KERNEL_SDF_CONSTRUCT = 8,                /* ConstructSignedDistanceField,         TressFXSDFCollision.hlsl:329-397 */
+    TFX_KERNEL_SDF_FINALIZE = 9,                 /* FinalizeSignedDistanceField,          TressFXSDFCollision.hlsl:400-412 */
+    TFX_KERNEL_SDF_COLLIDE = 10,                 /* CollideHairVerticesWithSdf_forward,   TressFXSDFCollision.hlsl:531-595 */
+    TFX_KERNEL_MESH_BONE_SKINNING = 11           /* BoneSkinning,                         TressFXBoneSkinning.hlsl:57-94 */
+} tfx_kernel;
+
+/* Buffer ids of a hair object (TressFXDynamicState + TressFXHairObject SRVs). */
+typedef enum tfx_buffer {
+    TFX_BUF_POSITIONS = 1,           /* float4[Vtot]  UAV  m_Positions                 */
+    TFX_BUF_POSITIONS_PREV = 2,      /* float4[Vtot]  UAV  m_PositionsPrev             */
+    TFX_BUF_POSITIONS_PREV_PREV = 3, /* float4[Vtot]  UAV  m_PositionsPrevPrev         */
+    TFX_BUF_TANGENTS = 4,            /* float4[Vtot]  UAV  m_Tangents                  */
+    TFX_BUF_STRAND_LEVEL_DATA = 5,   /* float4[3*Stot] UAV m_StrandLevelData           */
+    TFX_BUF_INITIAL_POSITIONS = 6,   /* float4[Vtot]  SRV  m_InitialHairPositionsBuffer */
+    TFX_BUF_REST_LENGTHS = 7,        /* float[Vtot]   SRV  m_HairRestLengthSRVBuffer    */
+    TFX_BUF_FOLLOW_ROOT_OFFSETS = 8, /* float4[Stot]  SRV  m_FollowHairRootOffsetBuffer */
+    TFX_BUF_BONE_SKINNING = 9        /* float4[2*Stot] SRV m_BoneSkinningDataBuffer     */
+} tfx_buffer;
+
+/* ---------------------------------------------------------------------------------- constants */
+/* Byte-for-byte TressFXSimulationParams (src/TressFX/TressFXConstantBuffers.h:41-85,
+ * capsules compiled out) = cbuffer tressfxSimParameters (TressFXSimulation.hlsl:49-79). */
+typedef struct tfx_sim_params {
+    float wind[4], wind1[4], wind2[4], wind3[4];
+    float shape[4];          /* damping, local stiffness, global stiffness, global range */
+    float grav_time_tip[4];  /* gravity magnitude, time step, tip separation            */
+    int32_t sim_ints[4];     /* length iterations, local iterations, collision flag     */
+    int32_t counts[4];       /* strands per thread group (64/n), follows per guide, n   */
+    float vsp[4];            /* VSP coefficient, VSP acceleration threshold             */
+    float reset_positions;
+    float clamp_position_delta;
+    float pad1, pad2;
+    float bone_matrices[TFX_MAX_BONES][16];
+} tfx_sim_params;
+
+/* TressFXSimulationSettings (src/TressFX/TressFXSettings.h:35-87), the user-facing knobs. */
+typedef struct tfx_sim_settings {
+    float vsp_coeff;
+    float vsp_accel_threshold;
+    float local_constraint_stiffness;
+    int32_t local_constraints_iterations;
+    float global_constraint_stiffness;
+    float global_constraints_range;
+    int32_t length_constraints_iterations;
+    float damping;
+    float gravity_magnitude;
+    float tip_separation;
+    float wind_magnitude;
+    float wind_direction[3];
+    float wind_angle_radians;
+    float clamp_position_delta;
+} tfx_sim_settings;
+
+/* Fill `settings` with the TressFXSimulationSettings defaults (TressFXSettings.h:38-56). */
+int tfx_sim_settings_default(tfx_sim_settings* settings);
+
+/* TressFXHairObject::UpdateSimulationParameters (TressFXHairObject.cpp:380-437) on a host-side
+ * constant block: writes every field it writes (wind via SetWind, :191-235), leaves the bone
+ * matrices alone, sets reset_positions = 1 when frame < 2, and returns the number of
+ * local-shape re-dispatches (m_CPULocalShapeIterations) in *cpu_local_iterations.
+ * Host-only: needs no device. */
+int tfx_fill_sim_params(tfx_sim_params* params, const tfx_sim_settings* settings, float time_step,
+                        int verts_per_strand, int follow_hairs_per_guide, int simulation_frame,
+                        int32_t* cpu_local_iterations);
+
+/* ---------------------------------------------------------------------------------- context */
+/* EI_Device + EI_CommandContext: selects `device` and creates a non-blocking stream. */
+int tfx_context_create(int device, tfx_context* out);
+int tfx_context_destroy(tfx_context ctx);
+/* Blocks until all work issued on the context's stream has finished (WaitForCompute). */
+int tfx_context_synchronize(tfx_context ctx);
+/* The context's cudaStream_t, as void*. */
+void* tfx_context_stream(tfx_context ctx);
+/* GetTimeStamp(name) (src/EngineInterface.h / DX12EngineInterfaceImpl.cpp:1319-1322): records a
+ * named CUDA event on the stream; tfx_context_timestamps returns up to `max` (name, ms since the
+ * first stamp) pairs of the completed stamps and clears the list. */
+int tfx_context_timestamp(tfx_context ctx, const char* name);
+int tfx_context_timestamps(tfx_context ctx, char (*names)[64], float* ms, int max, int* count);
+
+/* Page-locked host memory for overlapped uploads / read-backs (cudaHostAlloc, portable). */
+int tfx_host_alloc(size_t bytes, void** out);
+int tfx_host_free(void* ptr);
+
+/* ---------------------------------------------------------------------------------- hair object */
+typedef struct tfx_hair_desc {
+    int32_t num_guide_strands;     /* G: guide strands (m_numGuideStrands)                 */
+    int32_t verts_per_strand;      /* n in {4, 8, 16, 32, 64}                               */
+    int32_t follow_hairs_per_guide;/* F >= 0; Stot = G*(F+1), Vtot = Stot*n                 */
+    int32_t reserved;
+} tfx_hair_desc;
+
+/* TressFXHairObject ctor (TressFXHairObject.cpp:44-164) + TressFXDynamicState::CreateGPUResources
+ * / UploadGPUData (:502-558).  Host arrays are copied:
+ *   positions            float4[Vtot]   -> Pos, Prev, PrevPrev and InitialPositions
+ *   tangents             float4[Vtot]   -> Tangents (NULL = zeros)
+ *   rest_lengths         float[Vtot]    -> RestLength SRV
+ *   follow_root_offsets  float4[Stot]   -> RootOffset SRV (NULL = zeros)
+ *   bone_skinning        {float4 boneIndex, float4 boneWeight}[Stot] -> SkinningData SRV
+ * Validates n, index-space size, bone indices and weights of every guide strand. */
+int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* desc, const float* positions,
+                    const float* tangents, const float* rest_lengths, const float* follow_root_offsets,
+                    const float* bone_skinning, tfx_hair* out);
+int tfx_hair_destroy(tfx_hair hair);
+/* The host-side checks of tfx_hair_create without a device: n, index-space size, and the bone
+ * indices / weights of every guide strand exactly as ApplyVertexBoneSkinning reads them
+ * (TressFXSimulation.hlsl:552-564). Returns the status tfx_hair_create would return for them. */
+int tfx_hair_validate(const tfx_hair_desc* desc, const float* bone_skinning);
+/* TressFXHairObject::UpdateConstantBuffer (TressFXHairObject.cpp:375-378): uploads the scalar
+ * block and bone matrices [0, num_bones) of `params` for the next dispatches (stream ordered;
+ * the host block may be reused as soon as the call returns). counts must equal (64/n, F, n). */
+int tfx_hair_update_constants(tfx_hair hair, const tfx_sim_params* params, int num_bones);
+/* One EI Dispatch of a simulation kernel over the whole object (TressFXSimulation.cpp:51-75),
+ * repeated `repeat` times (the local-shape re-dispatch loop, :64-72). */
+int tfx_hair_dispatch(tfx_hair hair, int kernel, int repeat);
+/* TressFXSimulation::Simulate for one object (TressFXSimulation.cpp:77-112): the six stages in
+ * order, local shape dispatched `cpu_local_iterations` times. */
+int tfx_hair_simulate(tfx_hair hair, int cpu_local_iterations);
+/* Stream-ordered, blocking copies between a buffer and host memory (snapshot / restore). */
+int tfx_hair_read(tfx_hair hair, int buffer, void* host_dst, size_t bytes);
+int tfx_hair_write(tfx_hair hair, int buffer, const void* host_src, size_t bytes);
+/* Asynchronous variants: the caller keeps host memory alive (and pinned for overlap) until the
+ * stream reaches the copy. */
+int tfx_hair_read_async(tfx_hair hair, int buffer, void* host_dst, size_t bytes);
+int tfx_hair_write_async(tfx_hair hair, int buffer, const void* host_src, size_t bytes);
+/* Device address and byte size of a buffer (for a renderer or any interop). */
+int tfx_hair_get_buffer(tfx_hair hair, int buffer, void** device_ptr, size_t* bytes);
+/* out[0..3] = total vertices, total strands, vertices per strand, follow hairs per guide
+ * (GetNumTotalHairVertices / Strands / VerticesPerStrand / FollowHairsPerGuideHair). */
+int tfx_hair_get_counts(tfx_hair hair, int32_t out[4]);
+
+/* ---------------------------------------------------------------------------------- SDF */
+/* TressFXSDFCollisionParams (TressFXConstantBuffers.h:119-134), the grid part of it. */
+typedef struct tfx_sdf_grid {
+    float origin[4];
+    float cell_size;
+    int32_t num_cells_x, num_cells_y, num_cells_z;
+} tfx_sdf_grid;
+
+/* Grid sizing of the TressFXSDFCollision ctor (TressFXSDFCollision.cpp:38-86) from the mesh's
+ * initial bounding box: cell = (max.x-min.x)/numCellsInX, padding = (int)(0.8*numCellsInX)
+ * cells, dims = (int)((bbox + 2*padding)/cell), allocation = (int)(1.4*X*Y*Z) cells.
+ * Host-only. */
+int tfx_sdf_grid_from_bbox(const float bbox_min[3], const float bbox_max[3], int num_cells_in_x,
+                           tfx_sdf_grid* grid, float* padding, int64_t* alloc_cells);
+/* UpdateSDFGrid (TressFXSDFCollision.cpp:88-93): origin = current bbox min - padding. */
+int tfx_sdf_grid_origin(const float bbox_min[3], float padding, tfx_sdf_grid* grid);
+
+/* Allocates the grid buffer (uint32[alloc_cells], alloc_cells >= X*Y*Z of any grid used later). */
+int tfx_sdf_create(tfx_context ctx, int64_t alloc_cells, tfx_sdf* out);
+int tfx_sdf_destroy(tfx_sdf sdf);
+/* Binds the collision mesh (TressFXSDFInputMeshInterface::GetMeshBuffer /
+ * GetTrimeshVertexIndicesBuffer, TressFXSDFInputMeshInterface.h:38-48): borrowed DEVICE pointers
+ * to {float4 position, float4 normal}[num_vertices] and uint32[3*num_triangles]. */
+int tfx_sdf_set_mesh(tfx_sdf sdf, const void* mesh_vertices, int num_vertices, const uint32_t* indices,
+                     int num_triangles);
+/* TressFXSDFCollision::Update (TressFXSDFCollision.cpp:95-169): Initialize, Construct, Finalize
+ * on `grid` (cells X*Y*Z <= allocation). */
+int tfx_sdf_update(tfx_sdf sdf, const tfx_sdf_grid* grid);
+/* One SDF kernel alone (SDF_INITIALIZE / SDF_CONSTRUCT / SDF_FINALIZE) on `grid`. */
+int tfx_sdf_dispatch(tfx_sdf sdf, int kernel, const tfx_sdf_grid* grid);
+/* TressFXSDFCollision::CollideWithHair (TressFXSDFCollision.cpp:171-221): margin_world =
+ * collisionMargin * cellSize (:194), applied to every vertex of the object. */
+int tfx_sdf_collide(tfx_sdf sdf, tfx_hair hair, const tfx_sdf_grid* grid, float margin_world);
+int tfx_sdf_read(tfx_sdf sdf, void* host_dst, size_t bytes);
+int tfx_sdf_write(tfx_sdf sdf, const void* host_src, size_t bytes);
+int tfx_sdf_get_buffer(tfx_sdf sdf, void** device_ptr, size_t* bytes);
+
+/* ---------------------------------------------------------------------------------- collision mesh */
+/* TressFXBoneSkinning::Initialize (TressFXBoneSkinning.cpp:287-404): uploads the bind-pose mesh
+ * {float4 position, float4 normal}[num_vertices], uint32[3*num_triangles] and per-vertex
+ * {float4 boneIndex, float4 boneWeight}[num_vertices]. */
+int tfx_mesh_create(tfx_context ctx, const float* vertices, int num_vertices, const uint32_t* indices,
+                    int num_triangles, const float* bone_skinning, tfx_mesh* out);
+int tfx_mesh_destroy(tfx_mesh mesh);
+/* TressFXBoneSkinning::Update (TressFXBoneSkinning.cpp:460-504): uploads `num_bones` bone
+ * matrices and runs the BoneSkinning kernel into the skinned vertex buffer. */
+int tfx_mesh_skin(tfx_mesh mesh, const float* bone_matrices, int num_bones);
+/* Device pointers of the skinned vertex buffer and the index buffer (to feed tfx_sdf_set_mesh). */
+int tfx_mesh_get_buffers(tfx_mesh mesh, void** skinned_vertices, void** indices, int32_t* num_vertices,
+                         int32_t* num_triangles);
+int tfx_mesh_read_skinned(tfx_mesh mesh, float* host_dst, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRESSFX_GB300_H_ */

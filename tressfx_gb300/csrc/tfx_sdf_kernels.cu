@@ -1,0 +1,228 @@
+// Signed-distance-field kernels of the plain path (src/Shaders/TressFXSDFCollision.hlsl) and the
+// collision-mesh bone skinning kernel (src/Shaders/TressFXBoneSkinning.hlsl:57-94).
+//
+// The SDF grid is uint32[X*Y*Z] holding FloatFlip3-encoded distances while it is built (atomicMin
+// over the encoding = min |d|, ties to the positive value) and plain floats after Finalize.
+// atomicMin is order independent, and the distance arithmetic below is the reference's in the
+// same order with no FMA contraction, so the finished grid matches the oracle bit for bit.
+#include "tfx_device_math.cuh"
+#include "tfx_internal.h"
+
+namespace tfx {
+
+// FloatFlip3 / IFloatFlip3, TressFXSDFCollision.hlsl:92-100
+__device__ __forceinline__ uint32_t float_flip3(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u << 1) | (u >> 31);
+}
+__device__ __forceinline__ uint32_t ifloat_flip3(uint32_t u) { return (u >> 1) | (u << 31); }
+
+// GetSdfCoordinates, :103-113
+__device__ __forceinline__ int3 sdf_coords(const SdfGrid& g, float3 p) {
+    const float sx = (p.x - g.ox) / g.cell, sy = (p.y - g.oy) / g.cell, sz = (p.z - g.oz) / g.cell;
+    return make_int3(ftoi(sx), ftoi(sy), ftoi(sz));
+}
+// GetSdfCellPosition, :115-121
+__device__ __forceinline__ float3 sdf_cell_pos(const SdfGrid& g, int x, int y, int z) {
+    const float3 c = mk3((float)x * g.cell, (float)y * g.cell, (float)z * g.cell);
+    return add(c, mk3(g.ox, g.oy, g.oz));
+}
+
+// DistancePointToEdge, :147-159 (only the distance reaches the result)
+__device__ __forceinline__ float dist_point_edge(float3 p, float3 x0, float3 x1) {
+    const float3 x10 = sub(x1, x0);
+    float t = dot(sub(x1, p), x10) / dot(x10, x10);
+    t = fmaxf(0.0f, fminf(t, 1.0f));
+    const float3 a = sub(p, add(mul(t, x0), mul(1.0f - t, x1)));
+    return length(a);
+}
+
+// SignedDistancePointToTriangle, :163-215
+__device__ __forceinline__ float signed_dist_triangle(float3 p, float3 x0, float3 x1, float3 x2) {
+    float d;
+    float3 x02 = sub(x0, x2);
+    const float l0 = length(x02) + 1e-30f;
+    x02 = divs(x02, l0);
+    float3 x12 = sub(x1, x2);
+    const float l1 = dot(x12, x02);
+    x12 = sub(x12, mul(l1, x02));
+    const float l2 = length(x12) + 1e-30f;
+    x12 = divs(x12, l2);
+    const float3 px2 = sub(p, x2);
+    const float b = dot(x12, px2) / l2;
+    const float a = (dot(x02, px2) - l1 * b) / l0;
+    const float c = (1.0f - a) - b;
+    const float3 nTri = cross(sub(x1, x0), sub(x2, x0));
+    const float tol = 1e-8f;
+    if (a >= -tol && b >= -tol && c >= -tol) {
+        const float3 nn = sub(p, add(add(mul(a, x0), mul(b, x1)), mul(c, x2)));
+        d = length(nn);
+    } else {
+        d = dist_point_edge(p, x0, x1);
+        const float d12 = dist_point_edge(p, x1, x2);
+        const float d02 = dist_point_edge(p, x0, x2);
+        d = fminf(d, d12);
+        d = fminf(d, d02);
+    }
+    d = (dot(sub(p, x0), nTri) < 0.0f) ? -d : d;
+    return d;
+}
+
+// --------------------------------------------------------------------------------------------
+// InitializeSignedDistanceField, :301-312 (vectorised: 4 cells per 16 B store)
+__global__ void __launch_bounds__(256) k_sdf_initialize(uint32_t* __restrict__ sdf, long long cells) {
+    const uint32_t v = float_flip3(1e10f);
+    const long long n4 = cells >> 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    uint4* s4 = reinterpret_cast<uint4*>(sdf);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += stride) s4[i] = make_uint4(v, v, v, v);
+    for (long long i = (n4 << 2) + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells; i += stride) sdf[i] = v;
+}
+
+// ConstructSignedDistanceField, :329-397.  One thread per triangle.
+__global__ void __launch_bounds__(128) k_sdf_construct(uint32_t* __restrict__ sdf, SdfGrid g,
+                                                       const float4* __restrict__ mesh,
+                                                       const uint32_t* __restrict__ idx, int ntri) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const float3 tri0 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 0)));
+    const float3 tri1 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 1)));
+    const float3 tri2 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 2)));
+    const float3 m = mk3(g.cell, g.cell, g.cell);
+    const float3 aabbMin = sub(vmin(tri0, vmin(tri1, tri2)), m);
+    const float3 aabbMax = add(vmax(tri0, vmax(tri1, tri2)), m);
+    int3 lo = sdf_coords(g, aabbMin), hi = sdf_coords(g, aabbMax);
+    lo.x = max(0, min(lo.x - 1, g.nx - 1)); lo.y = max(0, min(lo.y - 1, g.ny - 1)); lo.z = max(0, min(lo.z - 1, g.nz - 1));
+    hi.x = max(0, min(hi.x + 1, g.nx - 1)); hi.y = max(0, min(hi.y + 1, g.ny - 1)); hi.z = max(0, min(hi.z + 1, g.nz - 1));
+    for (int z = lo.z; z <= hi.z; ++z)
+        for (int y = lo.y; y <= hi.y; ++y)
+            for (int x = lo.x; x <= hi.x; ++x) {
+                const long long ci = (long long)g.nx * g.ny * z + (long long)g.nx * y + x;
+                const float d = signed_dist_triangle(sdf_cell_pos(g, x, y, z), tri0, tri1, tri2);
+                atomicMin(sdf + ci, float_flip3(d));
+            }
+}
+
+// FinalizeSignedDistanceField, :400-412 (vectorised)
+__global__ void __launch_bounds__(256) k_sdf_finalize(uint32_t* __restrict__ sdf, long long cells) {
+    const long long n4 = cells >> 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    uint4* s4 = reinterpret_cast<uint4*>(sdf);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += stride) {
+        uint4 u = s4[i];
+        s4[i] = make_uint4(ifloat_flip3(u.x), ifloat_flip3(u.y), ifloat_flip3(u.z), ifloat_flip3(u.w));
+    }
+    for (long long i = (n4 << 2) + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells; i += stride)
+        sdf[i] = ifloat_flip3(sdf[i]);
+}
+
+// GetSignedDistance + TrilinearInterpolate, :414-527
+__device__ __forceinline__ float lerp_ref(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+__device__ __forceinline__ float sdf_lookup(const float* __restrict__ sdf, const SdfGrid& g, float3 p) {
+    const int3 gc = sdf_coords(g, p);
+    if (!(0 <= gc.x && gc.x < g.nx - 2) || !(0 <= gc.y && gc.y < g.ny - 2) || !(0 <= gc.z && gc.z < g.nz - 2))
+        return 1e10f;
+    const long long X = 1, Y = g.nx, Z = (long long)g.ny * g.nx;
+    const long long base = Z * gc.z + Y * gc.y + gc.x;
+    float d[8];
+    d[0] = __ldg(sdf + base);
+    d[1] = __ldg(sdf + base + X);
+    d[2] = __ldg(sdf + base + Y);
+    d[3] = __ldg(sdf + base + Y + X);
+    d[4] = __ldg(sdf + base + Z);
+    d[5] = __ldg(sdf + base + Z + X);
+    d[6] = __ldg(sdf + base + Z + Y);
+    d[7] = __ldg(sdf + base + Z + Y + X);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (d[j] == 1e10f) return 1e10f;
+    const float3 cp = sdf_cell_pos(g, gc.x, gc.y, gc.z);
+    const float3 ip = divs(sub(p, cp), g.cell);
+    const float b0 = lerp_ref(lerp_ref(d[0], d[1], ip.x), lerp_ref(d[2], d[3], ip.x), ip.y);
+    const float b1 = lerp_ref(lerp_ref(d[4], d[5], ip.x), lerp_ref(d[6], d[7], ip.x), ip.y);
+    return lerp_ref(b0, b1, ip.z);
+}
+
+// CollideHairVerticesWithSdf_forward, :531-595.  One thread per hair vertex (guides and follows).
+__global__ void __launch_bounds__(256) k_sdf_collide(const float* __restrict__ sdf, SdfGrid g, float margin,
+                                                     float4* __restrict__ pos, float4* __restrict__ prev,
+                                                     int n, long long vtot) {
+    const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (v >= vtot) return;
+    const int local = (int)(v % n);
+    if (local == 0 || local == 1) return;
+    const float4 hv = pos[v];
+    const float3 p = xyz(hv);
+    const float distance = sdf_lookup(sdf, g, p);
+    if (distance > margin) return;
+    const float h = 0.1f * g.cell;
+    const float fx = sdf_lookup(sdf, g, add(p, mul(mk3(1.0f, 0.0f, 0.0f), h)));
+    const float fy = sdf_lookup(sdf, g, add(p, mul(mk3(0.0f, 1.0f, 0.0f), h)));
+    const float fz = sdf_lookup(sdf, g, add(p, mul(mk3(0.0f, 0.0f, 1.0f), h)));
+    const float3 grad = mk3((fx - distance) / h, (fy - distance) / h, (fz - distance) / h);
+    const float3 nrm = normalize(grad);
+    if (distance < margin) {
+        const float3 proj = add(p, mul(nrm, margin - distance));
+        pos[v] = with_xyz(hv, proj);
+        const float4 pv = prev[v];
+        prev[v] = with_xyz(pv, proj);
+    }
+}
+
+// BoneSkinning, src/Shaders/TressFXBoneSkinning.hlsl:57-94.  One thread per mesh vertex.
+// in/out: {float4 position, float4 normal}; skin: {float4 boneIndex, float4 boneWeight}.
+__global__ void __launch_bounds__(256) k_mesh_skin(float4* __restrict__ out, const float4* __restrict__ in,
+                                                   const float4* __restrict__ skin, const float4* __restrict__ bones,
+                                                   int nverts) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nverts) return;
+    const float4 p = __ldg(in + 2 * v), nr = __ldg(in + 2 * v + 1);
+    float m[4][4];
+    blend_bones(bones, __ldg(skin + 2 * v), __ldg(skin + 2 * v + 1), m);
+    out[2 * v] = with_xyz(p, xform_row(xyz(p), 1.0f, m));
+    out[2 * v + 1] = with_xyz(nr, xform_row(xyz(nr), 0.0f, m));
+}
+
+// --------------------------------------------------------------------------------------------
+static inline unsigned grid_for(long long work, int threads, unsigned cap) {
+    long long b = (work + threads - 1) / threads;
+    if (b < 1) b = 1;
+    return (unsigned)(b > cap ? cap : b);
+}
+
+cudaError_t launch_sdf_initialize(uint32_t* sdf, int64_t cells, cudaStream_t s) {
+    if (cells <= 0) return cudaSuccess;
+    k_sdf_initialize<<<grid_for((cells + 3) / 4, 256, 152 * 16), 256, 0, s>>>(sdf, cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sdf_construct(uint32_t* sdf, const SdfGrid& g, const float4* mesh, const uint32_t* idx, int ntri,
+                                 cudaStream_t s) {
+    if (ntri <= 0) return cudaSuccess;
+    k_sdf_construct<<<(ntri + 127) / 128, 128, 0, s>>>(sdf, g, mesh, idx, ntri);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sdf_finalize(uint32_t* sdf, int64_t cells, cudaStream_t s) {
+    if (cells <= 0) return cudaSuccess;
+    k_sdf_finalize<<<grid_for((cells + 3) / 4, 256, 152 * 16), 256, 0, s>>>(sdf, cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sdf_collide(const uint32_t* sdf, const SdfGrid& g, float margin, float4* pos, float4* prev, int n,
+                               int64_t vtot, cudaStream_t s) {
+    if (vtot <= 0) return cudaSuccess;
+    k_sdf_collide<<<(unsigned)((vtot + 255) / 256), 256, 0, s>>>(reinterpret_cast<const float*>(sdf), g, margin, pos,
+                                                                 prev, n, vtot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_skin(float4* out, const float4* in, const float4* skin, const float4* bones, int nverts,
+                             cudaStream_t s) {
+    if (nverts <= 0) return cudaSuccess;
+    k_mesh_skin<<<(nverts + 255) / 256, 256, 0, s>>>(out, in, skin, bones, nverts);
+    return cudaGetLastError();
+}
+
+}  // namespace tfx

@@ -1,0 +1,106 @@
+"""Headless frame driver: the sample's per-frame order without a window.
+
+Simulation::StartSimulation (src/Simulation.cpp:50-94) runs, per frame:
+  1. skin every collision mesh (TressFXBoneSkinning::Update),
+  2. rebuild every SDF (TressFXSDFCollision::Update: Initialize, Construct, Finalize),
+  3. TressFXSimulation::Simulate over all hair objects (after UpdateBones),
+  4. collide every hair object with every SDF (TressFXSDFCollision::CollideWithHair).
+Before that, TressFXSample::UpdateSimulationParameters (src/TressFXSample.cpp:189-195) fills each
+object's constant block.  ``PlainPipeline`` issues exactly that sequence through the C ABI, one
+launch per object per stage.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _capi as A
+from .api import CollisionMesh, Context, HairObject, SDFCollision, Simulation, default_settings
+from .synthetic import Scene, SceneObject, margin_world, sdf_grid_for, wind_magnitude
+
+
+def settings_struct(d: dict) -> A.SimSettings:
+    s = default_settings()
+    for k, v in d.items():
+        if k == "wind_direction":
+            for i in range(3):
+                s.wind_direction[i] = float(v[i])
+        else:
+            setattr(s, k, v)
+    return s
+
+
+class FrameInputs:
+    """Everything the host feeds one frame: per-object settings, hair bones, mesh bones, SDF grid."""
+
+    def __init__(self, scene: Scene, frame: int):
+        t = frame * scene.dt
+        self.frame = frame
+        self.settings = []
+        self.hair_bones = []
+        self.mesh_bones = []
+        self.grids = []
+        for o in scene.objects:
+            st = dict(o.settings)
+            st["wind_magnitude"] = wind_magnitude(scene, o, frame)
+            self.settings.append(settings_struct(st))
+            self.hair_bones.append(o.bone_fn(t) if o.bone_fn is not None else np.eye(4, dtype=np.float32).reshape(1, 16))
+            if o.mesh is not None:
+                mb = o.mesh_bone_fn(t)
+                self.mesh_bones.append(mb)
+                self.grids.append(sdf_grid_for(o, mb))
+            else:
+                self.mesh_bones.append(None)
+                self.grids.append(None)
+
+
+class PlainPipeline:
+    """All objects of a scene on the plain path of one context."""
+
+    def __init__(self, ctx: Context, scene: Scene):
+        self.ctx = ctx
+        self.scene = scene
+        self.hair: list[HairObject] = []
+        self.meshes: list[CollisionMesh | None] = []
+        self.sdfs: list[SDFCollision | None] = []
+        self.sim = Simulation()
+        self.frame = 0
+        for o in scene.objects:
+            self.hair.append(HairObject(ctx, o.asset))
+            if o.mesh is not None:
+                m = CollisionMesh(ctx, o.mesh.vertices, o.mesh.indices, o.mesh.skinning)
+                s = SDFCollision(ctx, int(np.prod(o.sdf_dims)))
+                s.bind_mesh(m)
+                self.meshes.append(m)
+                self.sdfs.append(s)
+            else:
+                self.meshes.append(None)
+                self.sdfs.append(None)
+
+    def prepare(self, fin: FrameInputs) -> None:
+        """Host side of a frame: UpdateSimulationParameters + UpdateBones for every object."""
+        for h, st, hb in zip(self.hair, fin.settings, fin.hair_bones):
+            h.update_simulation_parameters(st, self.scene.dt)
+            h.update_bone_matrices(hb)
+
+    def run(self, fin: FrameInputs) -> None:
+        """Device side of a frame, stream ordered (skin, SDF, simulate, collide)."""
+        for m, s, mb, g in zip(self.meshes, self.sdfs, fin.mesh_bones, fin.grids):
+            if m is not None:
+                m.skin(mb)
+                s.update(g)
+        self.sim.simulate(self.hair)
+        for h, s, o, g in zip(self.hair, self.sdfs, self.scene.objects, fin.grids):
+            if s is not None:
+                s.collide(h, g, margin_world(o, g))
+        self.frame += 1
+
+    def step(self, frame: int | None = None) -> FrameInputs:
+        fin = FrameInputs(self.scene, self.frame if frame is None else frame)
+        self.prepare(fin)
+        self.run(fin)
+        return fin
+
+    def close(self) -> None:
+        for x in self.hair + self.meshes + self.sdfs:
+            if x is not None:
+                x.close()
