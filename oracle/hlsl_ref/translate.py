@@ -1,0 +1,93 @@
+"""Recipe: the reference's compute shaders -> C++ translation units (test infrastructure).
+
+Reads the reference's HLSL files where they lie and writes mechanically rewritten copies to
+oracle/_ref/ (git-ignored build output, never committed).  Only syntax the C++ compiler cannot
+accept is rewritten; every expression, statement and control-flow construct is kept as written.
+The rewrites, in order:
+
+  1. `[[vk::binding(..)]]`, `: register(..)`, `[numthreads(..)]` and `: SV_*` semantics removed;
+  2. `cbuffer Name { ... }` unwrapped: its members become globals of the translation unit;
+  3. `groupshared`, `row_major`, `column_major` removed (storage/packing qualifiers);
+  4. `inout T x` / `out T x` parameters become `T& x`;
+  5. un-suffixed floating literals get an `f` (HLSL literals take float type in float context);
+  6. `float4x4 name[N];` constant-buffer arrays become `HArray<float4x4, N> name;` (the shaders
+     index them with a float bone index);
+  7. the scalar swizzle `sharedLength[i].x` on a float array reads `sharedLength[i]`;
+  8. for TressFXBoneSkinning.hlsl only the compute part (up to the "// visualization" comment) is
+     kept; the vertex/pixel shaders after it are rendering code.
+
+The output is wrapped in a namespace per shader file and compiled against hlsl_shim.h.
+"""
+from __future__ import annotations
+
+import re
+import sys
+from pathlib import Path
+
+REF = Path("/root/reference")
+SHADERS = {
+    "ref_sim": "src/Shaders/TressFXSimulation.hlsl",
+    "ref_sdf": "src/Shaders/TressFXSDFCollision.hlsl",
+    "ref_skin": "src/Shaders/TressFXBoneSkinning.hlsl",
+}
+
+
+def _unwrap_cbuffers(s: str) -> str:
+    out = []
+    i = 0
+    pat = re.compile(r"cbuffer\s+\w+\s*\{")
+    while True:
+        m = pat.search(s, i)
+        if not m:
+            out.append(s[i:])
+            break
+        out.append(s[i:m.start()])
+        depth, j = 1, m.end()
+        while depth:
+            if s[j] == "{":
+                depth += 1
+            elif s[j] == "}":
+                depth -= 1
+            j += 1
+        out.append(s[m.end():j - 1])
+        i = j
+    return "".join(out)
+
+
+FLOAT_LIT = re.compile(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
+
+
+def translate(text: str, name: str) -> str:
+    s = text
+    if name == "ref_skin":
+        s = s.split("// visualization")[0]
+    s = re.sub(r"\[\[vk::binding\([^)]*\)\]\]", "", s)
+    s = re.sub(r":\s*register\s*\([^)]*\)", "", s)
+    s = re.sub(r"^\s*\[numthreads\([^)]*\)\]\s*$", "", s, flags=re.M)
+    s = re.sub(r":\s*SV_\w+", "", s)
+    s = _unwrap_cbuffers(s)
+    s = re.sub(r"\b(groupshared|row_major|column_major)\b", "", s)
+    s = re.sub(r"\binout\s+(\w+)\s+(\w+)", r"\1& \2", s)
+    s = re.sub(r"\bout\s+(\w+)\s+(\w+)", r"\1& \2", s)
+    s = FLOAT_LIT.sub(lambda m: m.group(1) + "f", s)
+    s = re.sub(r"\bfloat4x4\s+(\w+)\s*\[([^\]]+)\]\s*;", r"HArray<float4x4, \2> \1;", s)
+    s = re.sub(r"(sharedLength\[[^\]]+\])\.x\b", r"\1", s)
+    return f"// generated from {SHADERS[name]} by oracle/hlsl_ref/translate.py -- do not edit\n" \
+           f"namespace {name} {{\n{s}\n}}  // namespace {name}\n"
+
+
+def main(out_dir: Path) -> list[Path]:
+    out_dir.mkdir(parents=True, exist_ok=True)
+    written = []
+    for name, rel in SHADERS.items():
+        src = REF / rel
+        if not src.exists():
+            raise FileNotFoundError(src)
+        dst = out_dir / f"{name}.inc"
+        dst.write_text(translate(src.read_text(), name))
+        written.append(dst)
+    return written
+
+
+if __name__ == "__main__":
+    print(main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path(__file__).resolve().parent.parent / "_ref"))

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -63,12 +64,27 @@ extern "C" const char* tfx_last_error(void) { return g_last_error.c_str(); }
 extern "C" int tfx_abi_version(void) { return TFX_ABI_VERSION; }
 
 // ============================================================================ context
+// A context is reference counted: every hair object, SDF and mesh created on it holds a reference,
+// so tfx_context_destroy may be called before the objects are destroyed; the stream is released
+// with the last reference.
 struct tfx_context_t {
     int device = 0;
     cudaStream_t stream = nullptr;
+    std::atomic<int> refs{1};
     std::vector<std::string> stampNames;
     std::vector<cudaEvent_t> stampEvents;
 };
+
+static void context_retain(tfx_context c) { c->refs.fetch_add(1); }
+
+static void context_release(tfx_context c) {
+    if (c->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto ev : c->stampEvents) cudaEventDestroy(ev);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
 
 extern "C" int tfx_context_create(int device, tfx_context* out) {
     if (!out) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_context_create: out is null");
@@ -94,11 +110,7 @@ extern "C" int tfx_context_create(int device, tfx_context* out) {
 
 extern "C" int tfx_context_destroy(tfx_context c) {
     if (!c) return TFX_OK;
-    cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    for (auto ev : c->stampEvents) cudaEventDestroy(ev);
-    cudaStreamDestroy(c->stream);
-    delete c;
+    context_release(c);
     return TFX_OK;
 }
 
@@ -225,6 +237,7 @@ extern "C" int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* d, const fl
     auto* h = new (std::nothrow) tfx_hair_t();
     if (!h) return fail(TFX_ERR_OUT_OF_MEMORY, "tfx_hair_create: host allocation");
     h->ctx = ctx; h->G = (int)G; h->n = (int)n; h->F = (int)F; h->Vtot = Vtot; h->Stot = Stot;
+    context_retain(ctx);
 
     const size_t v16 = 16 * (size_t)Vtot, s16 = 16 * (size_t)Stot;
     const size_t sizes[10] = {0, v16, v16, v16, v16, 3 * s16, v16, 4 * (size_t)Vtot, s16, 2 * s16};
@@ -240,6 +253,7 @@ extern "C" int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* d, const fl
             if (h->staging[i]) cudaFreeHost(h->staging[i]);
             if (h->stagingDone[i]) cudaEventDestroy(h->stagingDone[i]);
         }
+        context_release(h->ctx);
         delete h;
     };
     cudaError_t e = cudaMalloc(&h->arena, total);
@@ -295,6 +309,7 @@ extern "C" int tfx_hair_destroy(tfx_hair h) {
         cudaFreeHost(h->staging[i]);
         cudaEventDestroy(h->stagingDone[i]);
     }
+    context_release(h->ctx);
     delete h;
     return TFX_OK;
 }
@@ -443,6 +458,7 @@ extern "C" int tfx_sdf_create(tfx_context ctx, int64_t alloc_cells, tfx_sdf* out
     if (e != cudaSuccess) { delete s; return cuda_fail(e, "tfx_sdf_create: cudaMalloc"); }
     e = cudaMemsetAsync(s->grid, 0, 4 * (size_t)alloc_cells, ctx->stream);
     if (e != cudaSuccess) { cudaFree(s->grid); delete s; return cuda_fail(e, "tfx_sdf_create: memset"); }
+    context_retain(ctx);
     *out = s;
     return TFX_OK;
 }
@@ -452,6 +468,7 @@ extern "C" int tfx_sdf_destroy(tfx_sdf s) {
     cudaSetDevice(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     cudaFree(s->grid);
+    context_release(s->ctx);
     delete s;
     return TFX_OK;
 }
@@ -566,6 +583,7 @@ extern "C" int tfx_mesh_destroy(tfx_mesh m) {
         if (m->staging[i]) cudaFreeHost(m->staging[i]);
         if (m->stagingDone[i]) cudaEventDestroy(m->stagingDone[i]);
     }
+    context_release(m->ctx);
     delete m;
     return TFX_OK;
 }
@@ -584,6 +602,7 @@ extern "C" int tfx_mesh_create(tfx_context ctx, const float* vertices, int nvert
     auto* m = new (std::nothrow) tfx_mesh_t();
     if (!m) return fail(TFX_ERR_OUT_OF_MEMORY, "tfx_mesh_create: host allocation");
     m->ctx = ctx; m->nverts = nverts; m->ntri = ntri;
+    context_retain(ctx);
     const size_t vb = 32 * (size_t)nverts, ib = 12 * (size_t)ntri, bb = 64 * (size_t)TFX_MAX_BONES;
     const size_t total = 3 * align256(vb) + align256(ib) + align256(bb);
     cudaError_t e = cudaMalloc(&m->arena, total);
