@@ -1,23 +1,29 @@
 """Benchmark: hair vertex-steps/s of TressFX strand simulation + SDF collision on one GB300.
 
-A step is one full frame of the per-frame pipeline on the synthetic "head" workload (20,000 guide
-strands x 32 vertices, 4 follow hairs per guide = 3.2 M vertices; 20k-triangle head mesh skinned
-by 3 joints; SDF 64^3 rebuilt every frame; 3 local-shape + 3 length iterations, VSP, wind with
-+-30 % noise): skin the collision mesh, rebuild the SDF, simulate, collide.
+A step is one full frame of the per-frame pipeline (Simulation::StartSimulation order): skin the
+collision meshes, rebuild the SDFs, simulate every hair object, collide.  Workloads (seeded,
+synthetic):
+  head     20,000 guides x 32 vertices, 4 follows per guide (3.2 M vertices), 20k-triangle head mesh
+           skinned by 3 joints, SDF 64^3 rebuilt every frame, 3 local-shape + 3 length iterations,
+           VSP, wind 2 m/s with +-30 % noise                                    [default]
+  fur      200,000 strands x 16 vertices, 50k-triangle torso, SDF 128^3, 2 + 2 iterations
+  batched  64 objects, strands log-uniform 512..50,000, n in {8,16,32,64}, per-object settings,
+           meshes of 5k..30k triangles and SDFs of 32^3..128^3
+  small    2,048 x 16, no SDF (the parity configuration)
 
-value  = vertices simulated per second over the timed frames, device time (CUDA events recorded on
-         the library's own stream), inputs resident in HBM.
-e2e    = the same metric through the public API with host buffers: every frame uploads its
-         constants (settings + bone matrices) and reads the simulated positions back into pinned
-         host memory; host wall clock with a synchronize per frame.
+value  = vertices simulated per second over exactly --steps timed frames of the batched path (one
+         CUDA-graph launch per frame), device time from CUDA events on the library's stream, inputs
+         resident in HBM.  The plain path (one launch per object per stage, the reference's dispatch
+         structure) is timed the same way and reported under "plain".
+e2e    = the same metric through the public C ABI with host buffers: every frame uploads its inputs
+         (constants, bone matrices, grids) from pinned memory and reads all simulated positions back
+         into pinned memory; host wall clock, synchronized every frame.
 --impl reference times the oracle (the CPU restatement of the reference shaders) on the host cores.
 """
 from __future__ import annotations
 
 import argparse
-import ctypes as C
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -31,6 +37,14 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+WORKLOADS = {
+    "head": "head 20000x32 F=4 (3.2M verts), 20k-tri mesh skinned by 3 joints, SDF 64^3, 3 local + 3 length iters, wind",
+    "fur": "fur 200000x16 (3.2M verts), 50k-tri torso, SDF 128^3, 2 local + 2 length iters",
+    "batched": "64 objects, strands log-uniform 512..50000 (x64 padded), n in {8,16,32,64}, SDF 32^3..128^3, "
+               "5k..30k-tri meshes (24.2M verts)",
+    "small": "plain small 2048x16, no SDF",
+}
+
 
 # ------------------------------------------------------------------------------------------ utils
 def load_peaks() -> dict:
@@ -42,7 +56,7 @@ def load_peaks() -> dict:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -57,10 +71,11 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            time.sleep(0.3)
         except FileNotFoundError:
             self.proc = None
         return self
@@ -98,28 +113,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# ------------------------------------------------------------------------------------------ workload
 def make_scene(name: str):
     from tressfx_gb300 import synthetic as S
-    if name == "head":
-        return S.scene_head()
-    if name == "fur":
-        return S.scene_fur()
-    if name == "small":
-        return S.scene_small()
-    raise SystemExit(f"unknown config {name}")
+    return {"head": S.scene_head, "fur": S.scene_fur, "small": S.scene_small, "batched": S.scene_batched}[name]()
 
 
-def algorithmic_bytes(scene) -> dict[str, float]:
-    """Algorithmic HBM bytes per frame of each kernel (each buffer element touched once)."""
+def plain_kernel_bytes(scene) -> dict[str, float]:
+    """Algorithmic HBM bytes per frame of each plain-path kernel (each element touched once)."""
     out: dict[str, float] = {}
+    add = lambda k, v: out.__setitem__(k, out.get(k, 0.0) + v)  # noqa: E731
     for o in scene.objects:
         a = o.asset
         G, n, F = a.num_guide_strands, a.verts_per_strand, a.follow_per_guide
         Vg, S, Vt = G * n, G, a.num_vertices
-        st = o.settings
-        cpu_it = st["local_constraints_iterations"] if n < 64 else 1
-        add = lambda k, v: out.__setitem__(k, out.get(k, 0.0) + v)  # noqa: E731
+        cpu_it = o.settings["local_constraints_iterations"] if n < 64 else 1
         add("IntegrationAndGlobalShapeConstraints", 96 * Vg + 32 * S)
         add("CalculateStrandLevelData", 196 * S)
         add("VelocityShockPropagation", 64 * Vg * (n - 2) / n + 32 * S)
@@ -137,21 +144,28 @@ def algorithmic_bytes(scene) -> dict[str, float]:
     return out
 
 
-# ------------------------------------------------------------------------------------------ GPU arm
-def run_gpu(args) -> dict:
+def fused_bytes(scene) -> dict[int, float]:
+    """Algorithmic HBM bytes per frame of the fused strand kernel of each n class: read Pos, Prev,
+    InitialPos, RestLength and write Pos, Prev, PrevPrev, Tangent of every guide vertex (116 B);
+    write Pos and Tangent of every follow vertex (32 B); per guide strand the skinning record, the
+    strand-level record and the follow root offsets."""
+    out: dict[int, float] = {}
+    for o in scene.objects:
+        a = o.asset
+        G, n, F = a.num_guide_strands, a.verts_per_strand, a.follow_per_guide
+        out[n] = out.get(n, 0.0) + 116 * G * n + 32 * F * G * n + G * (32 + 48 + 16 * F)
+    return out
+
+
+# ------------------------------------------------------------------------------------------ GPU legs
+def run_plain(ctx, scene, steps: int, warmup: int) -> dict:
     from tressfx_gb300 import _capi as A
-    from tressfx_gb300.api import Context
     from tressfx_gb300.headless import FrameInputs, PlainPipeline
     from tressfx_gb300.synthetic import margin_world
-
-    device = int(os.environ.get("LOCAL_RANK", "0"))
-    scene = make_scene(args.config)
-    ctx = Context(device)
     pipe = PlainPipeline(ctx, scene)
-    vpf = scene.vertices_per_frame
-
-    total = args.warmup + args.steps
-    inputs = [FrameInputs(scene, f) for f in range(total + args.steps)]
+    inputs = [FrameInputs(scene, f) for f in range(warmup + steps)]
+    names = ["IntegrationAndGlobalShapeConstraints", "CalculateStrandLevelData", "VelocityShockPropagation",
+             "LocalShapeConstraints", "LengthConstriantsWindAndCollision", "UpdateFollowHairVertices"]
 
     def frame(fin, stamps: bool) -> None:
         pipe.prepare(fin)
@@ -165,8 +179,6 @@ def run_gpu(args) -> dict:
                     st(nm + ">"); s.dispatch(k, g); st(nm + "<")
         for h in pipe.hair:
             h.update_constant_buffer()
-        names = ["IntegrationAndGlobalShapeConstraints", "CalculateStrandLevelData", "VelocityShockPropagation",
-                 "LocalShapeConstraints", "LengthConstriantsWindAndCollision", "UpdateFollowHairVertices"]
         for k, nm in zip(pipe.sim.STAGES, names):
             st(nm + ">")
             for h in pipe.hair:
@@ -178,97 +190,126 @@ def run_gpu(args) -> dict:
             if s is not None:
                 st("CollideHairVerticesWithSdf>"); s.collide(h, g, margin_world(o, g)); st("CollideHairVerticesWithSdf<")
 
-    launches_per_frame = 0
-    for o in scene.objects:
-        it = o.settings["local_constraints_iterations"] if o.asset.verts_per_strand < 64 else 1
-        launches_per_frame += 5 + it + (1 if o.asset.follow_per_guide > 0 else 0)
-        if o.mesh is not None:
-            launches_per_frame += 5
-
-    for f in range(args.warmup):
+    for f in range(warmup):
         frame(inputs[f], False)
     ctx.synchronize()
     ctx.timestamps()
-
-    # ---- device-timed region (stage stamps double as per-kernel timers)
-    with ClockSampler(device) as clocks:
-        ctx.timestamp("start")
-        for f in range(args.warmup, total):
-            frame(inputs[f], True)
-        ctx.timestamp("end")
-        ctx.synchronize()
-    stamps = ctx.timestamps(4096)
-    t_ms = stamps[-1][1] - stamps[0][1]
-    per_kernel: dict[str, list[float]] = {}
+    # whole-frame device time without inner stamps
+    ctx.timestamp("start")
+    for f in range(warmup, warmup + steps):
+        frame(inputs[f], False)
+    ctx.timestamp("end")
+    st = ctx.timestamps()
+    t_ms = st[-1][1] - st[0][1]
+    # one more pass with stamps around every stage for the per-kernel split
+    for f in range(warmup, warmup + min(steps, 20)):
+        frame(inputs[f], True)
+    stamps = ctx.timestamps(1 << 16)
+    per: dict[str, list[float]] = {}
     open_t: dict[str, float] = {}
-    for name, t in stamps[1:-1]:
+    for name, t in stamps:
         base, edge = name[:-1], name[-1]
         if edge == ">":
             open_t[base] = t
         else:
-            per_kernel.setdefault(base, []).append(t - open_t.pop(base))
+            per.setdefault(base, []).append(t - open_t.pop(base))
+    launches = 0
+    for o in scene.objects:
+        it = o.settings["local_constraints_iterations"] if o.asset.verts_per_strand < 64 else 1
+        launches += 5 + it + (1 if o.asset.follow_per_guide > 0 else 0) + (5 if o.mesh is not None else 0)
+    pipe.close()
+    nfr = min(steps, 20)
+    return {"ms_per_step": t_ms / steps, "value": scene.vertices_per_frame * steps / (t_ms * 1e-3),
+            "kernel_ms": {k: float(np.sum(v)) / nfr for k, v in per.items()}, "launches_per_frame": launches}
 
-    # ---- end-to-end through the public API with host buffers
+
+def run_batched(ctx, scene, steps: int, warmup: int, device: int, autotune: int) -> dict:
+    from tressfx_gb300 import _capi as A
     from tressfx_gb300.api import PinnedArray
+    from tressfx_gb300.headless import BatchedPipeline, FrameInputs
+    pipe = BatchedPipeline(ctx, scene, autotune_frames=autotune)
+    nframes = warmup + 2 * steps + 64
+    inputs = [FrameInputs(scene, f) for f in range(nframes)]
+    f = 0
+    for _ in range(warmup):
+        pipe.set_inputs(inputs[f]); pipe.run(inputs[f]); f += 1
+    ctx.synchronize()
+    desc, launches = pipe.batch.describe()
+
+    # ---- exactly `steps` timed frames (device time)
+    ctx.timestamps()
+    ctx.timestamp("start")
+    for _ in range(steps):
+        pipe.set_inputs(inputs[f % nframes]); pipe.run(inputs[f % nframes]); f += 1
+    ctx.timestamp("end")
+    st = ctx.timestamps()
+    t_ms = st[-1][1] - st[0][1]
+
+    # ---- clocks: the same frames repeated for about a second with the sampler running
+    with ClockSampler(device) as clocks:
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 1.2:
+            for _ in range(50):
+                pipe.set_inputs(inputs[f % nframes]); pipe.run(inputs[f % nframes]); f += 1
+            ctx.synchronize()
+
+    # ---- per-part split (direct launches with events between parts)
+    parts = []
+    for _ in range(min(steps, 10)):
+        pipe.set_inputs(inputs[f % nframes])
+        parts.append(pipe.batch.profile_frame())
+        for h in pipe.hair:
+            h.increase_simulation_frame()
+        f += 1
+    part_ms = np.median(np.array(parts), axis=0).tolist()
+
+    # ---- end to end with host buffers
     pinned = [PinnedArray((h.num_vertices, 4), np.float32) for h in pipe.hair]
-    e2e_frames = args.steps
     d2h = sum(p.array.nbytes for p in pinned)
     h2d = 0
     for h in pipe.hair:
         h2d += 128 + 64 * h.num_bones
     for o in scene.objects:
         if o.mesh is not None:
-            h2d += 64 * 3
+            h2d += 48 + 64 * 3
     ctx.synchronize()
     t0 = time.perf_counter()
-    for f in range(total, total + e2e_frames):
-        frame(inputs[f], False)
+    for _ in range(steps):
+        fin = inputs[f % nframes]
+        pipe.set_inputs(fin)
+        pipe.run(fin)
         for h, p in zip(pipe.hair, pinned):
             h.read_async(A.BUF_POSITIONS, p.array)
         ctx.synchronize()
+        f += 1
     e2e_s = time.perf_counter() - t0
     for p in pinned:
         p.free()
-
-    value = vpf * args.steps / (t_ms * 1e-3)
-    e2e = vpf * e2e_frames / e2e_s
-    peaks = load_peaks()
-    algo = algorithmic_bytes(scene)
-    kern_ms = {k: float(np.mean(v)) for k, v in per_kernel.items()}
-    dom = max(kern_ms, key=lambda k: kern_ms[k])
-    dom_bytes = algo.get(dom, 0.0)
-    achieved = dom_bytes / (kern_ms[dom] * 1e-3) / 1e9 if kern_ms[dom] > 0 else 0.0
-    res = {
-        "value": value, "ms_per_step": t_ms / args.steps, "e2e_value": e2e, "e2e_ms_per_step": e2e_s * 1e3 / e2e_frames,
-        "h2d": h2d, "d2h": d2h, "kernel_ms": kern_ms, "dominant": dom, "dominant_bytes": dom_bytes,
-        "achieved_gbs": achieved, "peak_gbs": peaks["hbm_gbs"], "peak_source": peaks["source"],
-        "clocks": clocks.summary(), "launches": launches_per_frame * args.steps, "scene": scene, "algo": algo,
-    }
     pipe.close()
-    ctx.close()
-    return res
+    return {"ms_per_step": t_ms / steps, "value": scene.vertices_per_frame * steps / (t_ms * 1e-3),
+            "e2e_value": scene.vertices_per_frame * steps / e2e_s, "e2e_ms_per_step": e2e_s * 1e3 / steps,
+            "h2d": h2d, "d2h": d2h, "part_ms": part_ms, "describe": desc, "launches_per_frame": launches,
+            "clocks": clocks.summary()}
 
 
 # ------------------------------------------------------------------------------------------ CPU legs
-def oracle_frames(scene, frames: int, min_seconds: float, max_seconds: float, threads: int) -> tuple[float, int]:
-    """Runs the oracle pipeline; returns (seconds, frames) of the bounded sample."""
+def oracle_sample(scene, min_seconds: float, max_seconds: float, threads: int) -> tuple[float, int]:
+    """Bounded sample of the oracle: full frames until min_seconds have elapsed (after one untimed
+    reset frame); returns (seconds, frames)."""
     from oracle.scene_driver import OraclePipeline
     from tressfx_gb300.headless import FrameInputs
     pipe = OraclePipeline(scene, np.float32, threads)
-    pipe.step(FrameInputs(scene, 0))   # untimed first frame (reset pose)
+    pipe.step(FrameInputs(scene, 0))
     done, t0 = 0, time.perf_counter()
     while True:
         pipe.step(FrameInputs(scene, 1 + done))
         done += 1
         el = time.perf_counter() - t0
-        if done >= frames and el >= min_seconds or el >= max_seconds:
+        if el >= min_seconds or el >= max_seconds:
             return el, done
 
 
 def run_reference(args) -> dict:
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return {}
     scene = make_scene(args.config)
     threads = os.cpu_count() or 1
     from oracle.scene_driver import OraclePipeline
@@ -280,86 +321,102 @@ def run_reference(args) -> dict:
     for f in range(args.warmup, args.warmup + args.steps):
         pipe.step(FrameInputs(scene, f))
     el = time.perf_counter() - t0
-    v = scene.vertices_per_frame * args.steps / el
-    return {"value": v, "ms_per_step": el * 1e3 / args.steps, "threads": threads, "scene": scene}
+    return {"value": scene.vertices_per_frame * args.steps / el, "ms_per_step": el * 1e3 / args.steps,
+            "threads": threads}
 
 
 # ------------------------------------------------------------------------------------------ main
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="head", choices=["head", "fur", "small"])
+    ap.add_argument("--config", default="head", choices=list(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--autotune", type=int, default=2, help="frames per candidate shape (0: defaults)")
+    ap.add_argument("--no-plain", action="store_true")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
-
+        dist.init_process_group("gloo")
     metric = "hair vertex-steps/s"
-    workload = {"head": "head 20000x32 F=4 (3.2M verts), 20k-tri mesh, SDF 64^3, 3 local + 3 length iters, wind",
-                "fur": "fur 200000x16 (3.2M verts), 50k-tri torso, SDF 128^3, 2 local + 2 length iters",
-                "small": "plain small 2048x16, no SDF"}[args.config]
+    base_cfg = {"workload": WORKLOADS[args.config], "parallelism": f"{world} replicas" if world > 1 else "single GPU",
+                "l2": "inputs larger than L2 (state of 3.2M+ vertices >= 256 MB per frame)"}
 
     if args.impl == "reference":
-        r = run_reference(args)
         if rank == 0:
+            r = run_reference(args)
             line = {"metric": metric, "value": r["value"], "unit": "vertex-steps/s", "n_gpus": args.gpus,
                     "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
                     "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                    "data": "synthetic (seeded)", "impl": "reference",
-                    "config": {"workload": workload, "parallelism": "replicas", "l2": "inputs larger than L2"},
-                    "cpu_baseline": {"value": r["value"], "unit": "vertex-steps/s", "cores": r["threads"], "kind": "port",
-                                     "sample": f"{args.steps} full frames of the workload after {args.warmup} warm-up frames"},
-                    "e2e": {"value": r["value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                    "data": "synthetic (seeded)", "impl": "reference", "config": base_cfg,
+                    "cpu_baseline": {"value": r["value"], "unit": "vertex-steps/s", "cores": r["threads"],
+                                     "kind": "port", "sample": f"{args.steps} full frames after {args.warmup} warm-up "
+                                                               f"frames, oracle restatement on all host threads"},
+                    "e2e": {"value": r["value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": 0,
+                            "d2h_bytes_per_step": 0}}
             print(json.dumps(line), flush=True)
         if dist is not None:
             dist.destroy_process_group()
         return
 
-    r = run_gpu(args)
-    # max over ranks of the device time
-    ms = r["ms_per_step"]
+    from tressfx_gb300.api import Context
+    scene = make_scene(args.config)
+    ctx = Context(local)
+    b = run_batched(ctx, scene, args.steps, args.warmup, local, args.autotune)
+    p = None if args.no_plain else run_plain(ctx, scene, min(args.steps, 100), args.warmup)
+    ms = b["ms_per_step"]
     if dist is not None:
         import torch
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{int(os.environ.get('LOCAL_RANK', '0'))}")
+        t = torch.tensor([ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = r["scene"].vertices_per_frame * world / (ms * 1e-3)
+    value = scene.vertices_per_frame * world / (ms * 1e-3)
 
     if rank == 0:
-        cpu = None
-        if world == 1 or rank == 0:
-            threads = os.cpu_count() or 1
-            el, fr = oracle_frames(r["scene"], 1, args.cpu_seconds, 4 * args.cpu_seconds, threads)
-            cpu = {"value": r["scene"].vertices_per_frame * fr / el, "unit": "vertex-steps/s", "cores": threads,
-                   "kind": "port", "sample": f"{fr} full frames of the workload after one untimed frame ({el:.1f} s)"}
-        dom = r["dominant"]
+        threads = os.cpu_count() or 1
+        el, fr = oracle_sample(scene, args.cpu_seconds, 4 * args.cpu_seconds, threads)
+        cpu = {"value": scene.vertices_per_frame * fr / el, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{fr} full frames of the workload after one untimed frame ({el:.1f} s, oracle restatement)"}
+        peaks = load_peaks()
+        fb = fused_bytes(scene)
+        classes = sorted(fb)
+        part = b["part_ms"]
+        kern = {"mesh_skin+sdf_build": part[0]}
+        for n, ms_k in zip(classes, part[1:]):
+            kern[f"fused_strands_n{n}"] = ms_k
+        dom_n = max(classes, key=lambda n: part[1 + classes.index(n)])
+        dom_ms = part[1 + classes.index(dom_n)]
+        achieved = fb[dom_n] / (dom_ms * 1e-3) / 1e9
         line = {
             "metric": metric, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": workload, "path": "plain (one launch per object per stage)",
-                       "parallelism": "replicas" if world > 1 else "single", "l2": "inputs larger than L2 (state 256 MB)"},
-            "e2e": {"value": r["e2e_value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": r["h2d"],
-                    "d2h_bytes_per_step": r["d2h"]},
-            "gpu_launches": r["launches"],
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": r["achieved_gbs"], "peak": r["peak_gbs"],
-                         "unit": "GB/s", "frac": r["achieved_gbs"] / r["peak_gbs"], "traffic": None,
-                         "peak_source": r["peak_source"], "algorithmic_bytes": r["dominant_bytes"]},
-            "kernel_ms": r["kernel_ms"],
+            "config": dict(base_cfg, path="batched: one CUDA graph per frame (mesh skinning, tiled SDF build, "
+                                          "fused persistent strand kernel per n class)", shapes=b["describe"]),
+            "e2e": {"value": b["e2e_value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": b["h2d"],
+                    "d2h_bytes_per_step": b["d2h"], "ms_per_step": b["e2e_ms_per_step"]},
+            "gpu_launches": b["launches_per_frame"] * args.steps,
+            "roofline": {"bound": "hbm", "kernel": f"k_fused_strands (n={dom_n})", "achieved": achieved,
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                         "peak_source": peaks["source"], "algorithmic_bytes": fb[dom_n], "launch_ms": dom_ms},
+            "kernel_ms": kern,
             "cpu_baseline": cpu,
-            "clocks": r["clocks"],
+            "clocks": dict(b["clocks"], window="the timed frames repeated for 1.2 s"),
         }
+        if p is not None:
+            line["plain"] = {"value": p["value"], "ms_per_step": p["ms_per_step"], "kernel_ms": p["kernel_ms"],
+                             "launches_per_frame": p["launches_per_frame"],
+                             "speedup_batched_vs_plain": p["ms_per_step"] / b["ms_per_step"]}
         print(json.dumps(line), flush=True)
+    ctx.close()
     if dist is not None:
         dist.destroy_process_group()
 

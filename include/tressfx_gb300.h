@@ -249,6 +249,47 @@ int tfx_mesh_get_buffers(tfx_mesh mesh, void** skinned_vertices, void** indices,
                          int32_t* num_triangles);
 int tfx_mesh_read_skinned(tfx_mesh mesh, float* host_dst, size_t bytes);
 
+/* ---------------------------------------------------------------------------------- batched path */
+/* The whole per-frame sequence of Simulation::StartSimulation (src/Simulation.cpp:50-94) for many
+ * objects at once: skin every collision mesh, rebuild every SDF, run TressFXSimulation::Simulate
+ * (TressFXSimulation.cpp:77-112) over every hair object and CollideWithHair
+ * (TressFXSDFCollision.cpp:171-221) for each object with its SDF -- as one CUDA-graph launch of a
+ * few persistent kernels instead of one dispatch per object per stage.  Results are bit-identical
+ * to the per-object dispatches above.  Objects keep their own buffers (tfx_hair_read / _get_buffer
+ * see the batched results); the mesh bound to an SDF must not change after tfx_batch_build. */
+typedef struct tfx_batch_t* tfx_batch;
+
+int tfx_batch_create(tfx_context ctx, tfx_batch* out);
+int tfx_batch_destroy(tfx_batch batch);
+/* Registers an SDF whose grid is nx*ny*nz cells every frame; `mesh` (or NULL for the mesh already
+ * bound with tfx_sdf_set_mesh) is skinned by the batch before the SDF is rebuilt. */
+int tfx_batch_add_sdf(tfx_batch batch, tfx_sdf sdf, tfx_mesh mesh, int nx, int ny, int nz, int* index);
+/* Registers a hair object that collides with SDF `sdf_index` (-1: no collision). */
+int tfx_batch_add_hair(tfx_batch batch, tfx_hair hair, int sdf_index, int* index);
+/* Builds the object / work / tile tables and captures the frame graphs (reserved must be 0). */
+int tfx_batch_build(tfx_batch batch, int reserved);
+/* Times the candidate launch shapes over `frames` frames each on the current inputs, restores every
+ * state buffer, and recaptures the graphs with the fastest shapes. */
+int tfx_batch_autotune(tfx_batch batch, int frames);
+/* Per-frame inputs (copied when tfx_batch_run is called): the constant block of hair object
+ * `index` (TressFXSimulationParams, bone matrices [0, num_bones)), and its local-shape
+ * re-dispatch count (m_CPULocalShapeIterations, TressFXHairObject.cpp:402-411). */
+int tfx_batch_set_hair_constants(tfx_batch batch, int index, const tfx_sim_params* params, int num_bones,
+                                 int cpu_local_iterations);
+/* This frame's grid of SDF `index` (dimensions fixed at tfx_batch_add_sdf) and its collision margin
+ * in world units (collisionMargin * cellSize). */
+int tfx_batch_set_sdf_frame(tfx_batch batch, int index, const tfx_sdf_grid* grid, float margin_world);
+/* This frame's bone matrices of the collision mesh of SDF `index`. */
+int tfx_batch_set_mesh_bones(tfx_batch batch, int index, const float* bone_matrices, int num_bones);
+/* Launches one frame on the context's stream (asynchronous). */
+int tfx_batch_run(tfx_batch batch);
+/* The launch shapes in use, as text, and the number of kernels one frame launches. */
+int tfx_batch_describe(tfx_batch batch, char* buf, size_t len, int32_t* launches_per_frame);
+/* Runs one frame like tfx_batch_run but with direct launches and CUDA events between its parts;
+ * waits for it and returns the milliseconds of each part: [0] = mesh skinning + SDF rebuild,
+ * [1..] = the fused strand launch of each vertices-per-strand class present (ascending n). */
+int tfx_batch_profile_frame(tfx_batch batch, float* part_ms, int max_parts, int* num_parts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,136 @@
+"""GPU parity of the batched path: one CUDA-graph launch per frame with fused persistent kernels
+and the tiled SDF build, against the FP32 oracle (and the plain path), bit for bit."""
+import numpy as np
+import pytest
+
+from oracle.scene_driver import OraclePipeline
+from tressfx_gb300 import _capi as A
+from tressfx_gb300.headless import BatchedPipeline, FrameInputs, PlainPipeline
+from tressfx_gb300.synthetic import scene_batched, scene_head, scene_small
+
+pytestmark = pytest.mark.gpu
+
+BUFS = [(A.BUF_POSITIONS, "pos"), (A.BUF_POSITIONS_PREV, "prev"), (A.BUF_POSITIONS_PREV_PREV, "prevprev"),
+        (A.BUF_TANGENTS, "tan"), (A.BUF_STRAND_LEVEL_DATA, "sld")]
+
+
+def assert_same(gpu_hair, ora_hair, what):
+    for buf, name in BUFS:
+        g = gpu_hair.read(buf).reshape(-1).view(np.uint32)
+        o = np.ascontiguousarray(getattr(ora_hair, name), dtype=np.float32).reshape(-1).view(np.uint32)
+        bad = np.nonzero(g != o)[0]
+        assert len(bad) == 0, f"{what}/{name}: {len(bad)} of {len(g)} words differ (first {bad[0]})"
+
+
+def run_pair(ctx, sc, frames, autotune=0):
+    gpu = BatchedPipeline(ctx, sc, autotune_frames=autotune)
+    ora = OraclePipeline(sc)
+    try:
+        for f in range(frames):
+            fin = gpu.step(f)
+            ora.step(fin)
+        for i, (h, oh) in enumerate(zip(gpu.hair, ora.hair)):
+            assert_same(h, oh, f"{sc.name} object {i}")
+        return gpu.batch.describe()
+    finally:
+        gpu.close()
+
+
+def test_batched_head_with_sdf(ctx):
+    sc = scene_head(seed=21, num_guides=300, n=32, follows=3, triangles=3000, sdf_cells=48, frames=6)
+    desc, launches = run_pair(ctx, sc, 6)
+    assert launches <= 8, desc
+
+
+@pytest.mark.parametrize("n", [4, 8, 16, 32, 64])
+def test_batched_every_strand_length(ctx, n):
+    sc = scene_small(seed=40 + n, num_guides=77, n=n)
+    sc.objects[0].settings.update(local_constraints_iterations=3, length_constraints_iterations=2, wind_magnitude=1.0)
+    run_pair(ctx, sc, 8)
+
+
+def test_batched_mixed_objects(ctx):
+    sc = scene_batched(seed=5, num_objects=7, min_strands=64, max_strands=700, min_tris=800, max_tris=3000,
+                       sdf_choices=(24, 32, 40), follows=1, frames=5)
+    run_pair(ctx, sc, 5)
+
+
+def test_batched_autotune_keeps_state(ctx):
+    sc = scene_batched(seed=6, num_objects=4, min_strands=64, max_strands=400, min_tris=800, max_tris=2000,
+                       sdf_choices=(24, 32), frames=4)
+    desc, _ = run_pair(ctx, sc, 4, autotune=2)
+    assert "vertices/lane" in desc
+
+
+def test_batched_equals_plain_path(ctx):
+    sc = scene_head(seed=22, num_guides=256, n=16, follows=2, triangles=2500, sdf_cells=40, frames=5)
+    a = PlainPipeline(ctx, sc)
+    b = BatchedPipeline(ctx, sc)
+    try:
+        for f in range(5):
+            a.step(f)
+            b.step(f)
+        for buf, name in BUFS:
+            assert np.array_equal(a.hair[0].read(buf).view(np.uint32), b.hair[0].read(buf).view(np.uint32)), name
+    finally:
+        a.close()
+        b.close()
+
+
+def test_batched_sdf_with_huge_triangles_falls_back_exactly(ctx):
+    """Triangles whose cell boxes cover most of the grid overflow the (triangle, tile) list; the
+    tile pass then scans every triangle and the grid is still exact."""
+    import oracle
+    from tressfx_gb300.synthetic import Mesh, SceneObject, Scene, build_asset, grow_strands, sample_on_ellipsoid, \
+        rigid_oscillation_bones
+    rng = np.random.default_rng(3)
+    v = np.zeros((4 + 3 * 400, 8), dtype=np.float32)
+    v[:4, :3] = [(-0.3, 1.3, -0.3), (0.3, 1.3, -0.3), (0.3, 1.9, 0.3), (-0.3, 1.9, 0.3)]
+    v[4:, :3] = rng.uniform(-0.12, 0.12, size=(1200, 3)) + np.array([0.0, 1.6, 0.0])
+    v[:, 3] = 1.0
+    idx = [0, 1, 2, 0, 2, 3] + list(range(4, 4 + 1200))
+    idx = np.array(idx, dtype=np.uint32)
+    skin = np.zeros((len(v), 8), dtype=np.float32)
+    skin[:, 4] = 1.0
+    mesh = Mesh(v, idx, skin)
+    roots, normals = sample_on_ellipsoid((0.0, 1.6, 0.0), (0.1, 0.1, 0.1), 64, rng)
+    asset = build_asset(grow_strands(roots, normals, 16, 0.006, 15.0, rng))
+    bones = rigid_oscillation_bones(10.0, 1.0, "y")
+    st = dict(vsp_coeff=0.8, vsp_accel_threshold=1.4, local_constraint_stiffness=0.9, local_constraints_iterations=1,
+              global_constraint_stiffness=0.0, global_constraints_range=0.0, length_constraints_iterations=1,
+              damping=0.08, gravity_magnitude=9.8, tip_separation=0.0, wind_magnitude=0.0, wind_direction=(1, 0, 0))
+    obj = SceneObject(asset, st, bones, mesh, bones, (40, 40, 40), 0.7 / 40, np.array([0.0, 1.6, 0.0]), follow_bone=0)
+    sc = Scene("huge_triangles", [obj], frames=3)
+    gpu = BatchedPipeline(ctx, sc)
+    ora = OraclePipeline(sc)
+    try:
+        for f in range(3):
+            fin = gpu.step(f)
+            ora.step(fin)
+        g = fin.grids[0]
+        words = gpu.sdfs[0].read(g.num_cells)
+        assert np.array_equal(words, ora.sdf_words[0])
+        assert_same(gpu.hair[0], ora.hair[0], "huge triangles")
+    finally:
+        gpu.close()
+
+
+def test_batch_rejects_bad_use(ctx):
+    from tressfx_gb300.api import Batch, HairObject
+    sc = scene_small(num_guides=64, n=16)
+    h = HairObject(ctx, sc.objects[0].asset)
+    b = Batch(ctx)
+    b.add_hair(h, -1)
+    with pytest.raises(A.TfxError):
+        b.add_hair(h, -1)            # twice
+    with pytest.raises(A.TfxError):
+        b.run()                      # not built
+    b.build()
+    with pytest.raises(A.TfxError):
+        b.run()                      # constants never set
+    p = h.current_params()
+    with pytest.raises(A.TfxError) as e:
+        b.set_hair_constants(0, p, 1, 1)   # counts of a never-filled block are zero
+    assert e.value.status == A.TFX_ERR_MISMATCH
+    b.close()
+    h.close()

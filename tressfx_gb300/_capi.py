@@ -164,6 +164,18 @@ _PROTOS = {
     "tfx_mesh_skin": (C.c_int, [P, P, C.c_int]),
     "tfx_mesh_get_buffers": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tfx_mesh_read_skinned": (C.c_int, [P, P, C.c_size_t]),
+    "tfx_batch_create": (C.c_int, [P, C.POINTER(P)]),
+    "tfx_batch_destroy": (C.c_int, [P]),
+    "tfx_batch_add_sdf": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "tfx_batch_add_hair": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_int)]),
+    "tfx_batch_build": (C.c_int, [P, C.c_int]),
+    "tfx_batch_autotune": (C.c_int, [P, C.c_int]),
+    "tfx_batch_set_hair_constants": (C.c_int, [P, C.c_int, C.POINTER(SimParams), C.c_int, C.c_int]),
+    "tfx_batch_set_sdf_frame": (C.c_int, [P, C.c_int, C.POINTER(SdfGrid), F32]),
+    "tfx_batch_set_mesh_bones": (C.c_int, [P, C.c_int, P, C.c_int]),
+    "tfx_batch_run": (C.c_int, [P]),
+    "tfx_batch_describe": (C.c_int, [P, C.c_char_p, C.c_size_t, C.POINTER(C.c_int32)]),
+    "tfx_batch_profile_frame": (C.c_int, [P, FP, C.c_int, C.POINTER(C.c_int)]),
 }
 
 EXPORTED_SYMBOLS = tuple(_PROTOS)

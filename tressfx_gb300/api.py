@@ -310,3 +310,71 @@ class SDFCollision:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """tfx_batch: many hair objects and their SDFs advanced by one CUDA-graph launch per frame."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(A.lib().tfx_batch_create(ctx.handle, C.byref(h)), "tfx_batch_create")
+        self.handle = h
+        self._keep = []
+
+    def add_sdf(self, sdf: SDFCollision, mesh: CollisionMesh | None, dims) -> int:
+        i = C.c_int()
+        check(A.lib().tfx_batch_add_sdf(self.handle, sdf.handle, mesh.handle if mesh is not None else None,
+                                        int(dims[0]), int(dims[1]), int(dims[2]), C.byref(i)), "tfx_batch_add_sdf")
+        self._keep += [sdf, mesh]
+        return i.value
+
+    def add_hair(self, hair: HairObject, sdf_index: int = -1) -> int:
+        i = C.c_int()
+        check(A.lib().tfx_batch_add_hair(self.handle, hair.handle, sdf_index, C.byref(i)), "tfx_batch_add_hair")
+        self._keep.append(hair)
+        return i.value
+
+    def build(self) -> None:
+        check(A.lib().tfx_batch_build(self.handle, 0), "tfx_batch_build")
+
+    def autotune(self, frames: int = 3) -> None:
+        check(A.lib().tfx_batch_autotune(self.handle, frames), "tfx_batch_autotune")
+
+    def set_hair_constants(self, index: int, params: A.SimParams, num_bones: int, cpu_local_iterations: int) -> None:
+        check(A.lib().tfx_batch_set_hair_constants(self.handle, index, C.byref(params), num_bones, cpu_local_iterations),
+              "tfx_batch_set_hair_constants")
+
+    def set_sdf_frame(self, index: int, grid: A.SdfGrid, margin_world: float) -> None:
+        check(A.lib().tfx_batch_set_sdf_frame(self.handle, index, C.byref(grid), float(margin_world)),
+              "tfx_batch_set_sdf_frame")
+
+    def set_mesh_bones(self, index: int, bones: np.ndarray) -> None:
+        b = np.ascontiguousarray(bones, dtype=np.float32).reshape(-1, 16)
+        check(A.lib().tfx_batch_set_mesh_bones(self.handle, index, ptr(b), len(b)), "tfx_batch_set_mesh_bones")
+
+    def run(self) -> None:
+        check(A.lib().tfx_batch_run(self.handle), "tfx_batch_run")
+
+    def profile_frame(self) -> list[float]:
+        ms = (C.c_float * 16)()
+        n = C.c_int()
+        check(A.lib().tfx_batch_profile_frame(self.handle, ms, 16, C.byref(n)), "tfx_batch_profile_frame")
+        return [float(ms[i]) for i in range(min(n.value, 16))]
+
+    def describe(self) -> tuple[str, int]:
+        buf = C.create_string_buffer(1024)
+        n = C.c_int32()
+        check(A.lib().tfx_batch_describe(self.handle, buf, 1024, C.byref(n)), "tfx_batch_describe")
+        return buf.value.decode(), n.value
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            A.lib().tfx_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass

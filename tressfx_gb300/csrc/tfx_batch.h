@@ -1,0 +1,76 @@
+// Structures of the batched path shared by its kernels (tfx_batch_kernels.cu) and its host side
+// (tfx_batch_capi.cu).
+#pragma once
+#include <algorithm>
+
+#include "tfx_internal.h"
+
+namespace tfx {
+
+// Per-frame grid of one SDF (origin moves with the follow bone) and the collision margin in world
+// units (collisionMargin * cellSize, TressFXSDFCollision.cpp:194).
+struct SdfFrame {
+    SdfGrid grid;
+    float margin;
+    float pad[3];
+};
+
+struct BatchObject {
+    HairView hair;                 // state buffers and counts of the hair object
+    const DevSimConsts* consts;    // this frame's constants (inside the device frame block)
+    const float* sdf;              // decoded SDF grid of the object's collision mesh, or null
+    const SdfFrame* sdfFrame;      // this frame's grid + margin (inside the device frame block)
+};
+
+// A group of up to 32 guide strands of one object: one block of the fused kernel at a time.
+struct WorkItem {
+    int obj;         // index into the object table
+    int firstGuide;  // first guide strand of the group
+    int count;       // guide strands in the group (<= 32)
+    int pad;
+};
+
+struct BatchMesh {
+    const float4* bind;     // {position, normal}[V]
+    float4* skinned;        // {position, normal}[V]
+    const float4* skin;     // {boneIndex, boneWeight}[V]
+    const float4* bones;    // this frame's bone matrices (inside the device frame block)
+    int firstVertex;        // prefix over meshes
+    int numVertices;
+    int pad[2];
+};
+
+struct BatchSdf {
+    const float4* mesh;       // skinned {position, normal}[V]
+    const uint32_t* indices;  // uint32[3T]
+    uint32_t* words;          // the grid: FloatFlip3 words while built, floats after
+    const SdfFrame* frame;    // grid of this frame
+    long long firstQuad;      // prefix over SDFs of ceil(cells / 4)
+    long long numCells;       // X*Y*Z
+    int firstTriangle;        // prefix over SDFs
+    int numTriangles;
+};
+
+struct FusedLaunch {
+    int n, vpl, warpsPerBlock, blocks;
+    const BatchObject* objs;
+    const WorkItem* items;
+    int numItems;
+};
+
+struct SdfBatchLaunch {
+    const BatchSdf* sdfs;
+    int nsdf;
+    int totalTris;
+    long long totalQuads;
+    int constructThreads;
+};
+
+cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s);
+cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s);
+cudaError_t launch_batch_sdf(const SdfBatchLaunch& l, cudaStream_t s);
+bool fused_config_valid(int n, int vpl);
+int fused_smem_bytes(int n, int vpl, int warps);
+int fused_blocks_per_sm(int n, int vpl, int warps);
+
+}  // namespace tfx

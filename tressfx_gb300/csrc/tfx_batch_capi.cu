@@ -1,0 +1,588 @@
+// C ABI of the batched path (tfx_batch_*): many hair objects and their SDFs advance one frame per
+// tfx_batch_run, which is one CUDA-graph launch.
+//
+// Frame layout.  Everything a frame needs from the host (each object's simulation constants and
+// bone matrices, each SDF's grid and margin, each collision mesh's bone matrices) lives in one
+// "frame block".  The caller fills a host copy with tfx_batch_set_*; tfx_batch_run copies it into
+// one of two pinned blocks and launches the graph that was captured for that block: its first
+// node uploads the block, then come the mesh skinning, the SDF rebuild and one fused strand launch
+// per vertices-per-strand class.  The two pinned blocks alternate, so the host can prepare frame
+// f+1 while frame f runs; an event per block keeps a block from being rewritten before its upload
+// has executed.
+//
+// Autotuning.  tfx_batch_autotune(b, frames) times the candidate launch shapes (vertices per lane
+// and warps per block of every fused class, block size of the SDF construct) on the real objects,
+// restores every state buffer it touched, and recaptures the graphs with the fastest shape of each
+// part.  All shapes give the same bits; only the speed differs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tfx_batch.h"
+#include "tfx_handles.h"
+
+using namespace tfx;
+
+struct BatchClass {
+    int n = 0;
+    int vpl = 1, warps = 8, blocks = 1;
+    std::vector<WorkItem> hostItems;
+    WorkItem* items = nullptr;  // device
+    int numItems = 0;
+};
+
+struct tfx_batch_t {
+    tfx_context ctx = nullptr;
+    std::vector<tfx_hair> hairs;
+    std::vector<int> hairSdf;
+    std::vector<bool> hairSet;
+    std::vector<tfx_sdf> sdfs;
+    std::vector<tfx_mesh> sdfMesh;
+    std::vector<int> sdfDims;  // 3 per SDF
+    std::vector<bool> sdfSet;
+    bool built = false;
+
+    // frame block
+    size_t blockBytes = 0;
+    std::vector<size_t> objOff, sdfOff, meshOff;
+    std::vector<int> objBones, meshBones;
+    std::vector<char> staging;
+    char* pinned[2] = {nullptr, nullptr};
+    char* devBlock = nullptr;
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    bool used[2] = {false, false};
+    int slot = 0;
+
+    // device tables
+    void* devArena = nullptr;
+    BatchObject* objTable = nullptr;
+    BatchMesh* meshTable = nullptr;
+    BatchSdf* sdfTable = nullptr;
+    int nmeshes = 0, totalMeshVerts = 0;
+    std::vector<BatchClass> classes;
+    SdfBatchLaunch sdfL{};
+
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int launchesPerFrame = 0;
+    std::string description;
+};
+
+static int batch_fail_built(const char* who) { return fail(TFX_ERR_INVALID_ARGUMENT, "%s: the batch is already built", who); }
+
+extern "C" int tfx_batch_create(tfx_context ctx, tfx_batch* out) {
+    if (!out || !ctx) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_create: null argument");
+    auto* b = new (std::nothrow) tfx_batch_t();
+    if (!b) return fail(TFX_ERR_OUT_OF_MEMORY, "tfx_batch_create: host allocation");
+    b->ctx = ctx;
+    context_retain(ctx);
+    *out = b;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_destroy(tfx_batch b) {
+    if (!b) return TFX_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    for (int i = 0; i < 2; ++i) {
+        if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
+        if (b->pinned[i]) cudaFreeHost(b->pinned[i]);
+        if (b->done[i]) cudaEventDestroy(b->done[i]);
+    }
+    if (b->devBlock) cudaFree(b->devBlock);
+    if (b->devArena) cudaFree(b->devArena);
+    for (auto& c : b->classes)
+        if (c.items) cudaFree(c.items);
+    for (auto h : b->hairs) context_release(h->ctx);
+    for (auto s : b->sdfs) context_release(s->ctx);
+    for (auto m : b->sdfMesh)
+        if (m) context_release(m->ctx);
+    context_release(b->ctx);
+    delete b;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_add_sdf(tfx_batch b, tfx_sdf sdf, tfx_mesh mesh, int nx, int ny, int nz, int* index) {
+    if (!b || !sdf) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_sdf: null argument");
+    if (b->built) return batch_fail_built("tfx_batch_add_sdf");
+    if (sdf->ctx != b->ctx || (mesh && mesh->ctx != b->ctx))
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_sdf: objects of another context");
+    if (nx <= 0 || ny <= 0 || nz <= 0 || (int64_t)nx * ny * nz > sdf->alloc)
+        return fail(TFX_ERR_SIZE, "tfx_batch_add_sdf: grid %dx%dx%d does not fit the SDF allocation", nx, ny, nz);
+    if (!mesh && (!sdf->mesh || sdf->ntri <= 0))
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_sdf: no mesh given and none bound to the SDF");
+    for (auto s : b->sdfs)
+        if (s == sdf) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_sdf: SDF added twice");
+    context_retain(sdf->ctx);
+    if (mesh) context_retain(mesh->ctx);
+    b->sdfs.push_back(sdf);
+    b->sdfMesh.push_back(mesh);
+    b->sdfDims.insert(b->sdfDims.end(), {nx, ny, nz});
+    b->sdfSet.push_back(false);
+    if (index) *index = (int)b->sdfs.size() - 1;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_add_hair(tfx_batch b, tfx_hair hair, int sdf_index, int* index) {
+    if (!b || !hair) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair: null argument");
+    if (b->built) return batch_fail_built("tfx_batch_add_hair");
+    if (hair->ctx != b->ctx) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair: object of another context");
+    if (sdf_index < -1 || sdf_index >= (int)b->sdfs.size())
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair: SDF index %d of %zu", sdf_index, b->sdfs.size());
+    for (auto h : b->hairs)
+        if (h == hair) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair: object added twice");
+    context_retain(hair->ctx);
+    b->hairs.push_back(hair);
+    b->hairSdf.push_back(sdf_index);
+    b->hairSet.push_back(false);
+    if (index) *index = (int)b->hairs.size() - 1;
+    return TFX_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+static void describe(tfx_batch b) {
+    char buf[1024];
+    int k = snprintf(buf, sizeof(buf), "sdf construct %d threads/block;", b->sdfL.constructThreads);
+    for (auto& c : b->classes)
+        k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of 32;",
+                      c.n, c.vpl, c.warps, c.blocks, c.numItems);
+    b->description = buf;
+}
+
+static void make_items(tfx_batch b, BatchClass& c) {
+    c.hostItems.clear();
+    for (int o = 0; o < (int)b->hairs.size(); ++o) {
+        tfx_hair h = b->hairs[o];
+        if (h->n != c.n) continue;
+        for (int g = 0; g < h->G; g += 32) c.hostItems.push_back(WorkItem{o, g, std::min(32, h->G - g), 0});
+    }
+    c.numItems = (int)c.hostItems.size();
+}
+
+static int upload_items(BatchClass& c) {
+    if (c.items) { cudaFree(c.items); c.items = nullptr; }
+    if (c.numItems == 0) return TFX_OK;
+    TFX_CUDA(cudaMalloc(&c.items, sizeof(WorkItem) * c.numItems), "tfx_batch: cudaMalloc items");
+    TFX_CUDA(cudaMemcpy(c.items, c.hostItems.data(), sizeof(WorkItem) * c.numItems, cudaMemcpyHostToDevice),
+             "tfx_batch: upload items");
+    return TFX_OK;
+}
+
+// Grid of a fused class: as many resident blocks as fit (persistent), no more than groups.
+static int size_class(tfx_batch b, BatchClass& c) {
+    const int perSM = fused_blocks_per_sm(c.n, c.vpl, c.warps);
+    if (perSM <= 0)
+        return fail(TFX_ERR_CUDA, "tfx_batch: fused kernel n=%d vpl=%d with %d warps cannot be resident", c.n, c.vpl, c.warps);
+    c.blocks = std::max(1, std::min(perSM * b->ctx->numSMs, c.numItems));
+    return TFX_OK;
+}
+
+static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* partMs) {
+    // the body of a frame without the block upload (used by capture, profiling and autotuning)
+    std::vector<cudaEvent_t> ev;
+    auto mark = [&]() {
+        if (!partMs) return;
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, s);
+        ev.push_back(e);
+    };
+    mark();
+    if (b->totalMeshVerts > 0) {
+        cudaError_t e = launch_batch_mesh_skin(b->meshTable, b->nmeshes, b->totalMeshVerts, s);
+        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: mesh skinning launch");
+    }
+    if (!b->sdfs.empty()) {
+        cudaError_t e = launch_batch_sdf(b->sdfL, s);
+        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: SDF launch");
+    }
+    mark();
+    for (auto& c : b->classes) {
+        if (c.numItems == 0) continue;
+        FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems};
+        cudaError_t e = launch_fused_strands(fl, s);
+        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: fused strand launch");
+        mark();
+    }
+    if (partMs) {
+        cudaEventSynchronize(ev.back());
+        partMs->clear();
+        for (size_t i = 1; i < ev.size(); ++i) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[i - 1], ev[i]);
+            partMs->push_back(t);
+        }
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+    return TFX_OK;
+}
+
+static int capture_graphs(tfx_batch b) {
+    cudaStream_t s = b->ctx->stream;
+    for (int slot = 0; slot < 2; ++slot) {
+        if (b->graph[slot]) { cudaGraphExecDestroy(b->graph[slot]); b->graph[slot] = nullptr; }
+        cudaGraph_t g = nullptr;
+        TFX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        cudaError_t e = cudaMemcpyAsync(b->devBlock, b->pinned[slot], b->blockBytes, cudaMemcpyHostToDevice, s);
+        int r = TFX_OK;
+        if (e != cudaSuccess) r = cuda_fail(e, "tfx_batch: capture upload");
+        if (r == TFX_OK) r = launch_frame_direct(b, s, nullptr);
+        cudaError_t ee = cudaStreamEndCapture(s, &g);
+        if (r != TFX_OK) { if (g) cudaGraphDestroy(g); return r; }
+        if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&b->graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    int launches = (b->totalMeshVerts > 0 ? 1 : 0) + (b->sdfs.empty() ? 0 : (b->sdfL.totalTris > 0 ? 3 : 2));
+    for (auto& c : b->classes) launches += c.numItems > 0 ? 1 : 0;
+    b->launchesPerFrame = launches;
+    return TFX_OK;
+}
+
+// State snapshot for the autotuner: every buffer a frame writes.
+struct Snapshot {
+    void* mem = nullptr;
+    std::vector<std::pair<void*, size_t>> regions;
+};
+
+static int snapshot_take(tfx_batch b, Snapshot& sn, cudaStream_t s) {
+    size_t total = 0;
+    sn.regions.clear();
+    for (auto h : b->hairs)
+        for (int k = TFX_BUF_POSITIONS; k <= TFX_BUF_STRAND_LEVEL_DATA; ++k) {
+            sn.regions.push_back({h->bufs[k].ptr, h->bufs[k].bytes});
+            total += align256(h->bufs[k].bytes);
+        }
+    for (size_t i = 0; i < b->sdfs.size(); ++i) {
+        sn.regions.push_back({b->sdfs[i]->grid, 4 * (size_t)b->sdfs[i]->alloc});
+        total += align256(4 * (size_t)b->sdfs[i]->alloc);
+        if (b->sdfMesh[i]) {
+            sn.regions.push_back({b->sdfMesh[i]->skinned, 32 * (size_t)b->sdfMesh[i]->nverts});
+            total += align256(32 * (size_t)b->sdfMesh[i]->nverts);
+        }
+    }
+    TFX_CUDA(cudaMalloc(&sn.mem, total ? total : 256), "tfx_batch: snapshot allocation");
+    char* p = (char*)sn.mem;
+    for (auto& r : sn.regions) {
+        TFX_CUDA(cudaMemcpyAsync(p, r.first, r.second, cudaMemcpyDeviceToDevice, s), "tfx_batch: snapshot");
+        p += align256(r.second);
+    }
+    return TFX_OK;
+}
+
+static int snapshot_restore(Snapshot& sn, cudaStream_t s) {
+    char* p = (char*)sn.mem;
+    for (auto& r : sn.regions) {
+        TFX_CUDA(cudaMemcpyAsync(r.first, p, r.second, cudaMemcpyDeviceToDevice, s), "tfx_batch: restore");
+        p += align256(r.second);
+    }
+    TFX_CUDA(cudaStreamSynchronize(s), "tfx_batch: restore sync");
+    cudaFree(sn.mem);
+    sn.mem = nullptr;
+    return TFX_OK;
+}
+
+static int autotune(tfx_batch b, int frames) {
+    cudaStream_t s = b->ctx->stream;
+    TFX_CUDA(cudaMemcpyAsync(b->devBlock, b->staging.data(), b->blockBytes, cudaMemcpyHostToDevice, s), "tfx_batch: upload");
+    Snapshot sn;
+    if (int r = snapshot_take(b, sn, s)) return r;
+    std::vector<float> part;
+    // best time of each part over `frames` frames with the current shapes
+    auto time_frames = [&](float* sdfMs, std::vector<float>* classMs) -> int {
+        float bestSdf = 1e30f;
+        std::vector<float> best(b->classes.size(), 1e30f);
+        for (int f = 0; f < frames; ++f) {
+            if (int r = launch_frame_direct(b, s, &part)) return r;
+            bestSdf = std::min(bestSdf, part[0]);
+            size_t k = 1;
+            for (size_t c = 0; c < b->classes.size(); ++c)
+                if (b->classes[c].numItems > 0 && k < part.size()) best[c] = std::min(best[c], part[k++]);
+        }
+        *sdfMs = bestSdf;
+        *classMs = best;
+        return TFX_OK;
+    };
+    int rc = TFX_OK;
+    if (!b->sdfs.empty() && b->sdfL.totalTris > 0) {
+        float bestMs = 1e30f;
+        int bestThreads = b->sdfL.constructThreads;
+        for (int th : {64, 128, 256}) {
+            b->sdfL.constructThreads = th;
+            float sdfMs;
+            std::vector<float> cm;
+            if ((rc = time_frames(&sdfMs, &cm))) break;
+            if (sdfMs < bestMs) { bestMs = sdfMs; bestThreads = th; }
+        }
+        b->sdfL.constructThreads = bestThreads;
+    }
+    for (size_t ci = 0; ci < b->classes.size() && rc == TFX_OK; ++ci) {
+        BatchClass& c = b->classes[ci];
+        if (c.numItems == 0) continue;
+        float bestMs = 1e30f;
+        int bestV = c.vpl, bestW = c.warps;
+        for (int vpl : {1, 2, 4}) {
+            if (!fused_config_valid(c.n, vpl)) continue;
+            for (int warps : {4, 8}) {
+                c.vpl = vpl;
+                c.warps = warps;
+                if (fused_blocks_per_sm(c.n, vpl, warps) <= 0) continue;
+                if ((rc = size_class(b, c))) break;
+                float sdfMs;
+                std::vector<float> cm;
+                if ((rc = time_frames(&sdfMs, &cm))) break;
+                if (cm[ci] < bestMs) { bestMs = cm[ci]; bestV = vpl; bestW = warps; }
+            }
+            if (rc) break;
+        }
+        c.vpl = bestV;
+        c.warps = bestW;
+        if (rc == TFX_OK) rc = size_class(b, c);
+    }
+    int rr = snapshot_restore(sn, s);
+    return rc ? rc : rr;
+}
+
+extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
+    if (!b) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_build: null batch");
+    if (b->built) return batch_fail_built("tfx_batch_build");
+    if (b->hairs.empty()) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_build: no hair objects");
+    if (reserved != 0) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_build: reserved must be 0");
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+
+    // ---- frame block layout
+    size_t off = 0;
+    for (auto h : b->hairs) {
+        b->objOff.push_back(off);
+        b->objBones.push_back(h->maxBone + 1);
+        off = align16(off + offsetof(DevSimConsts, bones) + 64 * (size_t)(h->maxBone + 1));
+    }
+    for (size_t i = 0; i < b->sdfs.size(); ++i) {
+        b->sdfOff.push_back(off);
+        off = align16(off + sizeof(SdfFrame));
+    }
+    for (size_t i = 0; i < b->sdfs.size(); ++i) {
+        tfx_mesh m = b->sdfMesh[i];
+        b->meshOff.push_back(off);
+        b->meshBones.push_back(m ? m->maxBone + 1 : 0);
+        if (m) off = align16(off + 64 * (size_t)(m->maxBone + 1));
+    }
+    b->blockBytes = std::max<size_t>(off, 16);
+    b->staging.assign(b->blockBytes, 0);
+    for (int i = 0; i < 2; ++i) {
+        TFX_CUDA(cudaMallocHost((void**)&b->pinned[i], b->blockBytes), "tfx_batch: pinned frame block");
+        TFX_CUDA(cudaEventCreateWithFlags(&b->done[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    TFX_CUDA(cudaMalloc((void**)&b->devBlock, b->blockBytes), "tfx_batch: device frame block");
+    TFX_CUDA(cudaMemset(b->devBlock, 0, b->blockBytes), "tfx_batch: clear frame block");
+
+    // ---- device tables
+    const int nobj = (int)b->hairs.size(), nsdf = (int)b->sdfs.size();
+    b->nmeshes = 0;
+    b->totalMeshVerts = 0;
+    for (auto m : b->sdfMesh)
+        if (m) { ++b->nmeshes; b->totalMeshVerts += m->nverts; }
+    const size_t sizes[3] = {sizeof(BatchObject) * nobj, sizeof(BatchMesh) * std::max(1, b->nmeshes),
+                             sizeof(BatchSdf) * std::max(1, nsdf)};
+    TFX_CUDA(cudaMalloc(&b->devArena, align256(sizes[0]) + align256(sizes[1]) + align256(sizes[2])), "tfx_batch: tables");
+    char* p = (char*)b->devArena;
+    b->objTable = (BatchObject*)p; p += align256(sizes[0]);
+    b->meshTable = (BatchMesh*)p; p += align256(sizes[1]);
+    b->sdfTable = (BatchSdf*)p;
+
+    std::vector<BatchObject> objs(nobj);
+    for (int o = 0; o < nobj; ++o) {
+        tfx_hair h = b->hairs[o];
+        objs[o].hair = h->view;
+        objs[o].consts = reinterpret_cast<const DevSimConsts*>(b->devBlock + b->objOff[o]);
+        const int si = b->hairSdf[o];
+        objs[o].sdf = si >= 0 ? reinterpret_cast<const float*>(b->sdfs[si]->grid) : nullptr;
+        objs[o].sdfFrame = si >= 0 ? reinterpret_cast<const SdfFrame*>(b->devBlock + b->sdfOff[si]) : nullptr;
+    }
+    TFX_CUDA(cudaMemcpy(b->objTable, objs.data(), sizeof(BatchObject) * nobj, cudaMemcpyHostToDevice), "tfx_batch: objects");
+
+    std::vector<BatchMesh> meshes;
+    int firstVertex = 0;
+    for (int i = 0; i < nsdf; ++i) {
+        tfx_mesh m = b->sdfMesh[i];
+        if (!m) continue;
+        BatchMesh d{};
+        d.bind = m->bind; d.skinned = m->skinned; d.skin = m->skin;
+        d.bones = reinterpret_cast<const float4*>(b->devBlock + b->meshOff[i]);
+        d.firstVertex = firstVertex; d.numVertices = m->nverts;
+        firstVertex += m->nverts;
+        meshes.push_back(d);
+    }
+    if (!meshes.empty())
+        TFX_CUDA(cudaMemcpy(b->meshTable, meshes.data(), sizeof(BatchMesh) * meshes.size(), cudaMemcpyHostToDevice),
+                 "tfx_batch: meshes");
+
+    std::vector<BatchSdf> sdfs(nsdf);
+    long long firstQuad = 0;
+    int firstTri = 0;
+    for (int i = 0; i < nsdf; ++i) {
+        tfx_sdf s = b->sdfs[i];
+        tfx_mesh m = b->sdfMesh[i];
+        BatchSdf& d = sdfs[i];
+        d.mesh = m ? m->skinned : s->mesh;
+        d.indices = m ? m->idx : s->idx;
+        d.numTriangles = m ? m->ntri : s->ntri;
+        d.words = s->grid;
+        d.frame = reinterpret_cast<const SdfFrame*>(b->devBlock + b->sdfOff[i]);
+        d.numCells = (long long)b->sdfDims[3 * i] * b->sdfDims[3 * i + 1] * b->sdfDims[3 * i + 2];
+        d.firstQuad = firstQuad;
+        d.firstTriangle = firstTri;
+        firstQuad += (d.numCells + 3) / 4;
+        firstTri += d.numTriangles;
+    }
+    if (nsdf > 0)
+        TFX_CUDA(cudaMemcpy(b->sdfTable, sdfs.data(), sizeof(BatchSdf) * nsdf, cudaMemcpyHostToDevice), "tfx_batch: SDFs");
+    b->sdfL = SdfBatchLaunch{b->sdfTable, nsdf, firstTri, firstQuad, 128};
+
+    // ---- strand classes (one fused launch per vertices-per-strand count present)
+    for (int n : {4, 8, 16, 32, 64}) {
+        bool any = false;
+        for (auto h : b->hairs) any |= (h->n == n);
+        if (!any) continue;
+        BatchClass c;
+        c.n = n;
+        c.vpl = n <= 32 ? 1 : 2;
+        c.warps = 8;
+        make_items(b, c);
+        if (int r = upload_items(c)) return r;
+        if (int r = size_class(b, c)) return r;
+        b->classes.push_back(std::move(c));
+    }
+    if (int r = capture_graphs(b)) return r;
+    b->built = true;
+    describe(b);
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_autotune(tfx_batch b, int frames) {
+    if (!b || !b->built || frames <= 0) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_autotune: batch not built or no frames");
+    for (size_t i = 0; i < b->hairSet.size(); ++i)
+        if (!b->hairSet[i]) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_autotune: constants of object %zu never set", i);
+    for (size_t i = 0; i < b->sdfSet.size(); ++i)
+        if (!b->sdfSet[i]) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_autotune: grid of SDF %zu never set", i);
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    TFX_CUDA(cudaStreamSynchronize(b->ctx->stream), "cudaStreamSynchronize");
+    if (int r = autotune(b, frames)) return r;
+    if (int r = capture_graphs(b)) return r;
+    describe(b);
+    return TFX_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+extern "C" int tfx_batch_set_hair_constants(tfx_batch b, int index, const tfx_sim_params* p, int num_bones,
+                                            int cpu_local_iterations) {
+    if (!b || !p || index < 0 || index >= (int)b->hairs.size())
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_hair_constants: bad argument");
+    if (!b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_hair_constants: build the batch first");
+    tfx_hair h = b->hairs[index];
+    if (p->counts[0] != TFX_THREAD_GROUP_SIZE / h->n || p->counts[1] != h->F || p->counts[2] != h->n)
+        return fail(TFX_ERR_MISMATCH, "tfx_batch_set_hair_constants: counts (%d,%d,%d) but object has (%d,%d,%d)", p->counts[0],
+                    p->counts[1], p->counts[2], TFX_THREAD_GROUP_SIZE / h->n, h->F, h->n);
+    if (num_bones < 0 || num_bones > TFX_MAX_BONES || cpu_local_iterations < 0 || cpu_local_iterations > 1024)
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_hair_constants: %d bones, %d local iterations", num_bones,
+                    cpu_local_iterations);
+    DevSimConsts* c = reinterpret_cast<DevSimConsts*>(b->staging.data() + b->objOff[index]);
+    fill_consts_header(c, p, cpu_local_iterations);
+    const int nb = std::min(num_bones, b->objBones[index]);
+    std::memcpy(reinterpret_cast<char*>(c) + offsetof(DevSimConsts, bones), p->bone_matrices, 64 * (size_t)nb);
+    b->hairSet[index] = true;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_set_sdf_frame(tfx_batch b, int index, const tfx_sdf_grid* g, float margin_world) {
+    if (!b || !g || index < 0 || index >= (int)b->sdfs.size())
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_sdf_frame: bad argument");
+    if (!b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_sdf_frame: build the batch first");
+    if (g->num_cells_x != b->sdfDims[3 * index] || g->num_cells_y != b->sdfDims[3 * index + 1] ||
+        g->num_cells_z != b->sdfDims[3 * index + 2] || !(g->cell_size > 0.0f))
+        return fail(TFX_ERR_MISMATCH, "tfx_batch_set_sdf_frame: grid %dx%dx%d (cell %g) differs from the batch's %dx%dx%d",
+                    g->num_cells_x, g->num_cells_y, g->num_cells_z, (double)g->cell_size, b->sdfDims[3 * index],
+                    b->sdfDims[3 * index + 1], b->sdfDims[3 * index + 2]);
+    SdfFrame* f = reinterpret_cast<SdfFrame*>(b->staging.data() + b->sdfOff[index]);
+    f->grid = SdfGrid{g->origin[0], g->origin[1], g->origin[2], g->cell_size, g->num_cells_x, g->num_cells_y,
+                      g->num_cells_z, 0};
+    f->margin = margin_world;
+    b->sdfSet[index] = true;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_set_mesh_bones(tfx_batch b, int index, const float* bones, int num_bones) {
+    if (!b || index < 0 || index >= (int)b->sdfs.size() || num_bones < 0 || (num_bones > 0 && !bones))
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_mesh_bones: bad argument");
+    if (!b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_mesh_bones: build the batch first");
+    if (!b->sdfMesh[index]) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_mesh_bones: SDF %d has no skinned mesh", index);
+    const int nb = std::min(num_bones, b->meshBones[index]);
+    std::memcpy(b->staging.data() + b->meshOff[index], bones, 64 * (size_t)nb);
+    return TFX_OK;
+}
+
+static int check_runnable(tfx_batch b, const char* who) {
+    if (!b || !b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "%s: batch not built", who);
+    for (size_t i = 0; i < b->hairSet.size(); ++i)
+        if (!b->hairSet[i]) return fail(TFX_ERR_INVALID_ARGUMENT, "%s: constants of object %zu never set", who, i);
+    for (size_t i = 0; i < b->sdfSet.size(); ++i)
+        if (!b->sdfSet[i]) return fail(TFX_ERR_INVALID_ARGUMENT, "%s: grid of SDF %zu never set", who, i);
+    return TFX_OK;
+}
+
+// Claims the next pinned block: waits until its previous upload has executed, then fills it.
+static int claim_block(tfx_batch b, int* slotOut) {
+    const int s = b->slot;
+    b->slot ^= 1;
+    if (b->used[s]) TFX_CUDA(cudaEventSynchronize(b->done[s]), "cudaEventSynchronize");
+    std::memcpy(b->pinned[s], b->staging.data(), b->blockBytes);
+    *slotOut = s;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_run(tfx_batch b) {
+    if (int r = check_runnable(b, "tfx_batch_run")) return r;
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    int s = 0;
+    if (int r = claim_block(b, &s)) return r;
+    TFX_CUDA(cudaGraphLaunch(b->graph[s], b->ctx->stream), "cudaGraphLaunch");
+    TFX_CUDA(cudaEventRecord(b->done[s], b->ctx->stream), "cudaEventRecord");
+    b->used[s] = true;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_profile_frame(tfx_batch b, float* part_ms, int max_parts, int* num_parts) {
+    if (!num_parts) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_profile_frame: null output");
+    if (int r = check_runnable(b, "tfx_batch_profile_frame")) return r;
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    cudaStream_t st = b->ctx->stream;
+    int s = 0;
+    if (int r = claim_block(b, &s)) return r;
+    TFX_CUDA(cudaMemcpyAsync(b->devBlock, b->pinned[s], b->blockBytes, cudaMemcpyHostToDevice, st), "tfx_batch: upload");
+    std::vector<float> part;
+    if (int r = launch_frame_direct(b, st, &part)) return r;
+    TFX_CUDA(cudaEventRecord(b->done[s], st), "cudaEventRecord");
+    b->used[s] = true;
+    const int k = std::min((int)part.size(), std::max(max_parts, 0));
+    for (int i = 0; i < k; ++i)
+        if (part_ms) part_ms[i] = part[i];
+    *num_parts = (int)part.size();
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_describe(tfx_batch b, char* buf, size_t len, int32_t* launches_per_frame) {
+    if (!b) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_describe: null batch");
+    if (buf && len) {
+        std::strncpy(buf, b->description.c_str(), len - 1);
+        buf[len - 1] = 0;
+    }
+    if (launches_per_frame) *launches_per_frame = b->launchesPerFrame;
+    return TFX_OK;
+}

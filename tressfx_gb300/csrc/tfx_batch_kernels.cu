@@ -1,0 +1,597 @@
+// Batched path kernels: many hair objects (uneven strand counts, vertices per strand, settings) and
+// their SDFs advance one frame in a handful of launches.
+//
+//  * k_batch_mesh_skin    - BoneSkinning (TressFXBoneSkinning.hlsl:57-94) over every vertex of every
+//                           collision mesh.
+//  * k_batch_sdf_init / k_batch_sdf_construct / k_batch_sdf_finalize
+//                         - InitializeSignedDistanceField / ConstructSignedDistanceField /
+//                           FinalizeSignedDistanceField (TressFXSDFCollision.hlsl:301-412) of every
+//                           SDF.  The construct runs one warp per triangle: the lanes share the
+//                           triangle's cell box (the reference's AABB +- one cell, -+ one grid cell),
+//                           the triangle-only terms of the distance are computed once, and each
+//                           (triangle, cell) pair does the reference's distance and an atomicMin on the
+//                           FloatFlip3 word.  The pairs and the encoding are the reference's, so the grid
+//                           is bit-identical.
+//  * k_fused_strands      - the six simulation stages (TressFXSimulation.hlsl:609-1001) and the SDF
+//                           collision (TressFXSDFCollision.hlsl:531-595) of a group of 32 guide
+//                           strands in one pass.  Phase 1 (all warps, L = n/VPL lanes per strand):
+//                           integration + global shape, strand-level data, VSP; positions and
+//                           bind-pose positions go to shared memory.  Phase 2 (warp 0, one lane per
+//                           strand): the local-shape sweeps, with the iterations software-pipelined
+//                           as a wavefront (iteration k runs two vertices behind iteration k-1, which
+//                           is exactly the order in which the sequential sweeps read and write).
+//                           Phase 3 (all warps): wind, length constraints (warp shuffles), tangents,
+//                           velocity clamp, follow hairs, collision, and the single write of every
+//                           buffer.  Blocks are persistent over the strand groups of every object of
+//                           one vertices-per-strand class.
+// All per-vertex arithmetic is the reference's, in the same order, so every buffer matches the
+// plain path and the oracle bit for bit.
+#include "tfx_batch.h"
+#include "tfx_sdf_math.cuh"
+
+namespace tfx {
+
+// ============================================================================================
+// collision-mesh skinning over all meshes
+__global__ void __launch_bounds__(256) k_batch_mesh_skin(const BatchMesh* __restrict__ meshes, int nmeshes,
+                                                         int totalVerts) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= totalVerts) return;
+    int lo = 0, hi = nmeshes - 1;
+    while (lo < hi) {  // last mesh with firstVertex <= t
+        const int mid = (lo + hi + 1) >> 1;
+        if (meshes[mid].firstVertex <= t) lo = mid; else hi = mid - 1;
+    }
+    const BatchMesh& m = meshes[lo];
+    const int v = t - m.firstVertex;
+    const float4 p = __ldg(m.bind + 2 * v), nr = __ldg(m.bind + 2 * v + 1);
+    float mm[4][4];
+    blend_bones(m.bones, __ldg(m.skin + 2 * v), __ldg(m.skin + 2 * v + 1), mm);
+    m.skinned[2 * v] = with_xyz(p, xform_row(xyz(p), 1.0f, mm));
+    m.skinned[2 * v + 1] = with_xyz(nr, xform_row(xyz(nr), 0.0f, mm));
+}
+
+// ============================================================================================
+// SDF rebuild of every SDF
+__device__ __forceinline__ int find_by_prefix_tri(const BatchSdf* __restrict__ sdfs, int nsdf, long long t) {
+    int lo = 0, hi = nsdf - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sdfs[mid].firstTriangle <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ int find_by_prefix_quad(const BatchSdf* __restrict__ sdfs, int nsdf, long long q) {
+    int lo = 0, hi = nsdf - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sdfs[mid].firstQuad <= q) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// InitializeSignedDistanceField, :301-312: every cell of every SDF, 4 cells per thread (the last
+// quad of an SDF may be partial).
+__global__ void __launch_bounds__(256) k_batch_sdf_init(const BatchSdf* __restrict__ sdfs, int nsdf, long long totalQuads) {
+    const uint32_t v = float_flip3(1e10f);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < totalQuads; q += stride) {
+        const BatchSdf& s = sdfs[find_by_prefix_quad(sdfs, nsdf, q)];
+        const long long c = 4 * (q - s.firstQuad);
+        const long long cells = s.numCells;
+        uint32_t* g = s.words;
+        if (c + 4 <= cells) {
+            *reinterpret_cast<uint4*>(g + c) = make_uint4(v, v, v, v);
+        } else {
+            for (long long i = c; i < cells; ++i) g[i] = v;
+        }
+    }
+}
+
+// FinalizeSignedDistanceField, :400-412
+__global__ void __launch_bounds__(256) k_batch_sdf_finalize(const BatchSdf* __restrict__ sdfs, int nsdf,
+                                                            long long totalQuads) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < totalQuads; q += stride) {
+        const BatchSdf& s = sdfs[find_by_prefix_quad(sdfs, nsdf, q)];
+        const long long c = 4 * (q - s.firstQuad);
+        const long long cells = s.numCells;
+        uint32_t* g = s.words;
+        if (c + 4 <= cells) {
+            uint4 u = *reinterpret_cast<uint4*>(g + c);
+            *reinterpret_cast<uint4*>(g + c) = make_uint4(ifloat_flip3(u.x), ifloat_flip3(u.y), ifloat_flip3(u.z),
+                                                          ifloat_flip3(u.w));
+        } else {
+            for (long long i = c; i < cells; ++i) g[i] = ifloat_flip3(g[i]);
+        }
+    }
+}
+
+// ConstructSignedDistanceField, :329-397, one warp per triangle.
+__global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __restrict__ sdfs, int nsdf, int totalTris) {
+    const int warpsTotal = gridDim.x * (blockDim.x >> 5);
+    const int lane = threadIdx.x & 31;
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < totalTris; t += warpsTotal) {
+        const BatchSdf& s = sdfs[find_by_prefix_tri(sdfs, nsdf, t)];
+        const SdfGrid g = s.frame->grid;
+        const int tri = t - s.firstTriangle;
+        const float3 x0 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 0)));
+        const float3 x1 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 1)));
+        const float3 x2 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 2)));
+        int3 lo, hi;
+        tri_cell_box(g, x0, x1, x2, lo, hi);
+        const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
+        const int vol = nx * ny * nz;
+        const TriPre P = tri_pre(x0, x1, x2);
+        for (int c = lane; c < vol; c += 32) {
+            const int x = lo.x + c % nx, y = lo.y + (c / nx) % ny, z = lo.z + c / (nx * ny);
+            const float d = signed_dist_pre(sdf_cell_pos(g, x, y, z), P);
+            atomicMin(s.words + ((long long)z * g.ny + y) * g.nx + x, float_flip3(d));
+        }
+    }
+}
+
+// ============================================================================================
+// fused strand kernel
+//
+// Shared memory of one block (one group of 32 strands of n vertices; rows padded to 33 strands so
+// the sweep lanes and the vertex-parallel accesses are both conflict free):
+//   SP[n][33] float4  positions   SV[n][33] float4  Prev   BX/BY/BZ[n][33] float  bind-pose positions
+__host__ __device__ constexpr int fused_smem_for(int n) { return n * 33 * (16 + 16 + 12); }
+
+// One step of LocalShapeConstraints (TressFXSimulation.hlsl:794-825) for vertex j: pm1/pos are the
+// strand's vertices j-1 and j as this sweep has left them, pp1 vertex j+1 as the previous sweep left
+// it, bm1/b0/bp1 the bind-pose positions.  Updates pos (final for j) and pp1.
+__device__ __forceinline__ void local_shape_step(float4 pm1, float4& pos, float4& pp1, float3 bm1, float3 b0, float3 bp1,
+                                                 float stiff) {
+    const float3 lastVec = sub(xyz(pos), xyz(pm1));
+    const float3 vecBindPose = sub(bp1, b0);
+    const float3 lastVecBindPose = sub(b0, bm1);
+    const Q4 rg = qfrom2(normalize(lastVecBindPose), normalize(lastVec));
+    const float3 org = add(qrot(rg, vecBindPose), xyz(pos));
+    const float3 del = mul(stiff, sub(org, xyz(pp1)));
+    if (pos.w > 0.0f) { pos.x = pos.x - del.x; pos.y = pos.y - del.y; pos.z = pos.z - del.z; }
+    if (pp1.w > 0.0f) { pp1.x = pp1.x + del.x; pp1.y = pp1.y + del.y; pp1.z = pp1.z + del.z; }
+}
+
+// Barrier among the first `threads` threads of the block (named barrier 1; all of them must call it).
+__device__ __forceinline__ void bar_sync_first(int threads) {
+    asm volatile("bar.sync 1, %0;" ::"r"(threads) : "memory");
+}
+
+// KW consecutive local-shape sweeps of the block's strands, as a wavefront over warps: warp k
+// (k < KW) runs sweep k, lane s is strand s, and at time step t warp k works on vertex
+// j = t - 2k + 1.  Sweep k needs vertex j+1 as sweep k-1 left it, which warp k-1 stored at step t-1;
+// within one step no two warps touch the same element, and a barrier of the KW warps separates the
+// steps, so every read sees exactly the value the sequential sweeps give it.
+__device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const float* __restrict__ BX,
+                                                const float* __restrict__ BY, const float* __restrict__ BZ, int s,
+                                                bool active, int n, int k, int KW, float stiff) {
+    constexpr int LD = 33;
+    float4 pm1 = make_float4(0.f, 0.f, 0.f, 0.f), pos = pm1;
+    float3 bm1 = mk3(0.f, 0.f, 0.f), b0 = bm1;
+    const int T = (n - 2) + 2 * (KW - 1);
+    for (int t = 0; t < T; ++t) {
+        const int j = t - 2 * k + 1;
+        if (active && j >= 1 && j <= n - 2) {
+            if (j == 1) {
+                pm1 = SP[s]; pos = SP[LD + s];
+                bm1 = mk3(BX[s], BY[s], BZ[s]);
+                b0 = mk3(BX[LD + s], BY[LD + s], BZ[LD + s]);
+            }
+            float4 pp1 = SP[(j + 1) * LD + s];
+            const float3 bp1 = mk3(BX[(j + 1) * LD + s], BY[(j + 1) * LD + s], BZ[(j + 1) * LD + s]);
+            local_shape_step(pm1, pos, pp1, bm1, b0, bp1, stiff);
+            SP[j * LD + s] = pos;
+            if (j == n - 2) SP[(n - 1) * LD + s] = pp1;
+            pm1 = pos; pos = pp1; bm1 = b0; b0 = bp1;
+        }
+        bar_sync_first(KW * 32);
+    }
+}
+
+template <int N, int VPL>
+__global__ void __launch_bounds__(256) k_fused_strands(const BatchObject* __restrict__ objs,
+                                                       const WorkItem* __restrict__ items, int numItems) {
+    constexpr int L = N / VPL;      // lanes per strand in the vertex phases
+    constexpr int SPW = 32 / L;     // strands per warp pass
+    constexpr int LD = 33;
+    extern __shared__ float4 smem_f4[];
+    float4* SP = smem_f4;                                       // [N][LD]
+    float4* SV = SP + N * LD;                                   // [N][LD]
+    float* BX = reinterpret_cast<float*>(SV + N * LD);          // [N][LD] x3
+    float* BY = BX + N * LD;
+    float* BZ = BY + N * LD;
+
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int q = lane % L;         // lane within the strand
+    const int slot = lane / L;      // strand slot within the warp pass
+    const int segBase = slot * L;   // first lane of this strand
+
+    for (int it = blockIdx.x; it < numItems; it += gridDim.x) {
+        const WorkItem wi = items[it];
+        const BatchObject& ob = objs[wi.obj];
+        const HairView& h = ob.hair;
+        const DevSimConsts* __restrict__ c = ob.consts;
+        const int F = h.F;
+        const float dt = c->timeStep;
+
+        // ============================================================ phase 1
+        for (int pass = warp; pass * SPW < wi.count; pass += nwarps) {
+            const int s = pass * SPW + slot;   // strand within the group
+            const bool active = s < wi.count;
+            const int g = wi.firstGuide + s;
+            const int gs = g * (F + 1);
+            const int base = gs * N + q * VPL;
+            float4 p[VPL], pv[VPL], ppv[VPL], ip[VPL];
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                if (active) {
+                    p[k] = h.pos[base + k];
+                    ppv[k] = h.prev[base + k];
+                    ip[k] = __ldg(h.init + base + k);
+                } else {
+                    p[k] = ppv[k] = ip[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+            const float4 sidx = active ? __ldg(h.skin + 2 * gs) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 swt = active ? __ldg(h.skin + 2 * gs + 1) : make_float4(1.f, 0.f, 0.f, 0.f);
+            float m[4][4];
+            blend_bones(c->bones, sidx, swt, m);
+
+            // IntegrationAndGlobalShapeConstraints
+            const bool reset = c->reset != 0.0f;
+            const float kG = c->globalStiffness, range = c->globalRange;
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                const int j = q * VPL + k;
+                float4 initialPos = ip[k];
+                const float3 sk = xform_row(xyz(initialPos), 1.0f, m);
+                initialPos.x = sk.x; initialPos.y = sk.y; initialPos.z = sk.z;
+                float4 currentPos = p[k];
+                float4 shared = currentPos;
+                float4 oldPos = ppv[k];
+                if (reset) { currentPos = initialPos; oldPos = initialPos; }
+                if (currentPos.w > 0.0f) {
+                    const float gx = c->gravity * 0.0f, gy = c->gravity * -1.0f;
+                    const float3 cur = xyz(currentPos), old = xyz(oldPos);
+                    const float3 force = mk3(gx, gy, gx);
+                    const float3 r = add(add(cur, mul(c->decay, sub(cur, old))), mul(mul(force, dt), dt));
+                    shared.x = r.x; shared.y = r.y; shared.z = r.z;
+                } else {
+                    shared = initialPos;
+                }
+                if (kG > 0.0f && range != 0.0f) {
+                    if (shared.w > 0.0f) {
+                        if ((float)j < range * (float)N) {
+                            const float3 del = mul(kG, sub(xyz(initialPos), xyz(shared)));
+                            shared.x = shared.x + del.x; shared.y = shared.y + del.y; shared.z = shared.z + del.z;
+                        }
+                    }
+                }
+                pv[k] = currentPos;
+                p[k] = shared;
+                if (active) h.prevprev[base + k] = ppv[k];
+            }
+
+            // CalculateStrandLevelData: vertices 0 and 1 after integration
+            float4 oo1, o0, o1, n0, n1;
+            if constexpr (VPL == 1) {
+                const int l1 = segBase + 1;
+                oo1 = shfl4(ppv[0], l1); o1 = shfl4(pv[0], l1); n1 = shfl4(p[0], l1);
+                o0 = shfl4(pv[0], segBase); n0 = shfl4(p[0], segBase);
+            } else {
+                oo1 = shfl4(ppv[1], segBase); o1 = shfl4(pv[1], segBase); n1 = shfl4(p[1], segBase);
+                o0 = shfl4(pv[0], segBase); n0 = shfl4(p[0], segBase);
+            }
+            const float3 u = normalize(sub(xyz(o1), xyz(o0)));
+            const float3 v = normalize(sub(xyz(n1), xyz(n0)));
+            const Q4 rot = qfrom2(u, v);
+            const float3 trans = sub(xyz(n0), qrot(rot, xyz(o0)));
+            float vspCoeff = c->vspCoeff;
+            {
+                const float ax = (n1.x - 2.0f * o1.x) + oo1.x;
+                const float ay = (n1.y - 2.0f * o1.y) + oo1.y;
+                const float az = (n1.z - 2.0f * o1.z) + oo1.z;
+                const float aw = (n1.w - 2.0f * o1.w) + oo1.w;
+                const float accel = sqrtf(ax * ax + ay * ay + az * az + aw * aw);
+                if (accel > c->vspAccelThreshold) vspCoeff = 1.0f;
+            }
+            const Q4 bq = quat_from_matrix(m);
+            if (active && q == 0) {
+                h.sld[3 * gs + 0] = make_float4(bq.x, bq.y, bq.z, bq.w);
+                h.sld[3 * gs + 1] = make_float4(rot.x, rot.y, rot.z, rot.w);
+                h.sld[3 * gs + 2] = make_float4(trans.x, trans.y, trans.z, vspCoeff);
+            }
+
+            // VelocityShockPropagation, then hand over to shared memory
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                const int j = q * VPL + k;
+                if (j >= 2) {
+                    const float3 a = add(mul(1.0f - vspCoeff, xyz(p[k])), mul(vspCoeff, add(qrot(rot, xyz(p[k])), trans)));
+                    const float3 b = add(mul(1.0f - vspCoeff, xyz(pv[k])), mul(vspCoeff, add(qrot(rot, xyz(pv[k])), trans)));
+                    p[k] = with_xyz(p[k], a);
+                    pv[k] = with_xyz(pv[k], b);
+                }
+                if (active) {
+                    SP[j * LD + s] = p[k];
+                    SV[j * LD + s] = pv[k];
+                    const float3 bp = qrot(bq, xyz(ip[k]));
+                    BX[j * LD + s] = bp.x; BY[j * LD + s] = bp.y; BZ[j * LD + s] = bp.z;
+                }
+            }
+        }
+        __syncthreads();
+
+        // ============================================================ phase 2: LocalShapeConstraints
+        const int lsIters = c->reserved0;
+        if (lsIters > 0) {
+            const float stiff = 0.5f * fminf(c->localStiffness, 0.95f);
+            for (int done = 0; done < lsIters;) {   // waves of up to one sweep per warp
+                const int KW = min(lsIters - done, nwarps);
+                if (warp < KW) sweep_wavefront(SP, BX, BY, BZ, lane, lane < wi.count, N, warp, KW, stiff);
+                __syncthreads();
+                done += KW;
+            }
+        } else {
+            __syncthreads();
+        }
+
+        // ============================================================ phase 3
+        const float* sdf = ob.sdf;
+        SdfGrid sg;
+        float margin = 0.0f;
+        if (sdf) {
+            sg = ob.sdfFrame->grid;
+            margin = ob.sdfFrame->margin;
+        }
+        for (int pass = warp; pass * SPW < wi.count; pass += nwarps) {
+            const int s = pass * SPW + slot;
+            const bool active = s < wi.count;
+            const int g = wi.firstGuide + s;
+            const int gs = g * (F + 1);
+            const int base = gs * N + q * VPL;
+            float4 p[VPL], pv[VPL], tn[VPL];
+            float len[VPL];
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                const int j = q * VPL + k;
+                if (active) {
+                    p[k] = SP[j * LD + s];
+                    pv[k] = SV[j * LD + s];
+                    tn[k] = h.tan[base + k];
+                    len[k] = __ldg(h.rest + base + k);
+                } else {
+                    p[k] = pv[k] = tn[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    len[k] = 0.0f;
+                }
+            }
+            // wind: every displacement from the pre-wind positions
+            if (c->anyWind) {
+                const float a = (float)(gs % 20) / 20.0f;
+                const float3 w = add(add(add(mul(a, xyz(c->wind[0])), mul(1.0f - a, xyz(c->wind[1]))),
+                                         mul(a, xyz(c->wind[2]))),
+                                     mul(1.0f - a, xyz(c->wind[3])));
+                float4 nxt[VPL];
+#pragma unroll
+                for (int k = 0; k + 1 < VPL; ++k) nxt[k] = p[k + 1];
+                nxt[VPL - 1] = shfl4_down(p[0], 1);
+                float3 disp[VPL];
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) {
+                    const int j = q * VPL + k;
+                    disp[k] = mk3(0.f, 0.f, 0.f);
+                    if (j >= 2 && j < N - 1) {
+                        const float3 vv = sub(xyz(p[k]), xyz(nxt[k]));
+                        const float3 force = neg(cross(cross(vv, w), vv));
+                        disp[k] = mul(mul(force, dt), dt);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) {
+                    const int j = q * VPL + k;
+                    if (j >= 2 && j < N - 1) {
+                        p[k].x = p[k].x + disp[k].x; p[k].y = p[k].y + disp[k].y; p[k].z = p[k].z + disp[k].z;
+                    }
+                }
+            }
+            // length constraints
+            const int lenIters = c->lengthIterations;
+            for (int iter = 0; iter < lenIters; ++iter) {
+                if constexpr (VPL == 1) {
+                    {
+                        const float4 o = shfl4(p[0], lane ^ 1);
+                        const float ol = __shfl_sync(FULL, len[0], lane ^ 1);
+                        const bool even = (q & 1) == 0;
+                        const DC r = even ? distance_constraint(p[0], o, len[0]) : distance_constraint(o, p[0], ol);
+                        p[0] = even ? r.p0 : r.p1;
+                    }
+                    {
+                        const bool odd = (q & 1) != 0;
+                        const int src = odd ? ((lane + 1) & 31) : ((lane + 31) & 31);
+                        const float4 o = shfl4(p[0], src);
+                        const float ol = __shfl_sync(FULL, len[0], src);
+                        if (odd && q <= N - 3) p[0] = distance_constraint(p[0], o, len[0]).p0;
+                        else if (!odd && q >= 2) p[0] = distance_constraint(o, p[0], ol).p1;
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < VPL; k += 2) {
+                        const DC r = distance_constraint(p[k], p[k + 1], len[k]);
+                        p[k] = r.p0; p[k + 1] = r.p1;
+                    }
+#pragma unroll
+                    for (int k = 1; k + 1 < VPL; k += 2) {
+                        const DC r = distance_constraint(p[k], p[k + 1], len[k]);
+                        p[k] = r.p0; p[k + 1] = r.p1;
+                    }
+                    const float4 nextFirst = shfl4_down(p[0], 1);
+                    const float4 prevLast = shfl4_up(p[VPL - 1], 1);
+                    const float prevLen = __shfl_up_sync(FULL, len[VPL - 1], 1);
+                    const float4 myLast = p[VPL - 1];
+                    const float4 myFirst = p[0];
+                    if (q < L - 1) p[VPL - 1] = distance_constraint(myLast, nextFirst, len[VPL - 1]).p0;
+                    if (q >= 1) p[0] = distance_constraint(prevLast, myFirst, prevLen).p1;
+                }
+            }
+            // tangents
+            {
+                const float4 nx = shfl4_down(p[0], 1);
+                const float4 pvl = shfl4_up(p[VPL - 1], 1);
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) {
+                    const int j = q * VPL + k;
+                    float3 t;
+                    if (j == N - 1) {
+                        const float4 before = (k > 0) ? p[k > 0 ? k - 1 : 0] : pvl;
+                        t = sub(xyz(p[k]), xyz(before));
+                    } else {
+                        const float4 after = (k + 1 < VPL) ? p[k + 1 < VPL ? k + 1 : k] : nx;
+                        t = sub(xyz(after), xyz(p[k]));
+                    }
+                    tn[k] = with_xyz(tn[k], normalize(t));
+                }
+            }
+            // velocity clamp
+            const float clamp2 = c->clamp * c->clamp;
+#pragma unroll
+            for (int k = 0; k < VPL; ++k) {
+                float3 d = sub(xyz(p[k]), xyz(pv[k]));
+                const float speedSqr = dot(d, d);
+                if (speedSqr > clamp2) {
+                    d = mul(d, clamp2 / speedSqr);
+                    pv[k] = with_xyz(pv[k], sub(xyz(p[k]), d));
+                }
+            }
+            if (active) {
+                // UpdateFollowHairVertices from the constrained guide, each follow collided at once
+                const float tip = c->tipSeparation;
+                for (int i = 0; i < F; ++i) {
+                    const int fs = gs + i + 1;
+                    const float4 off = __ldg(h.followOffset + fs);
+#pragma unroll
+                    for (int k = 0; k < VPL; ++k) {
+                        const int j = q * VPL + k;
+                        const int fv = fs * N + j;
+                        const float factor = tip * ((float)j / (float)N) + 1.0f;
+                        float3 fp = add(xyz(p[k]), mul(factor, xyz(off)));
+                        const float4 oldF = h.pos[fv];
+                        h.tan[fv] = tn[k];
+                        float3 proj;
+                        if (sdf && j >= 2 && sdf_collide_point(sdf, sg, margin, fp, proj)) {
+                            fp = proj;
+                            const float4 pf = h.prev[fv];
+                            h.prev[fv] = with_xyz(pf, proj);
+                        }
+                        h.pos[fv] = with_xyz(oldF, fp);
+                    }
+                }
+                // guide collision and the final writes
+#pragma unroll
+                for (int k = 0; k < VPL; ++k) {
+                    const int j = q * VPL + k;
+                    float3 proj;
+                    if (sdf && j >= 2 && sdf_collide_point(sdf, sg, margin, xyz(p[k]), proj)) {
+                        p[k] = with_xyz(p[k], proj);
+                        pv[k] = with_xyz(pv[k], proj);
+                    }
+                    h.pos[base + k] = p[k];
+                    h.prev[base + k] = pv[k];
+                    h.tan[base + k] = tn[k];
+                }
+            }
+        }
+        __syncthreads();   // shared memory is reused by the next group
+    }
+}
+
+// ============================================================================================
+// host launch helpers
+template <int N, int VPL>
+static cudaError_t launch_fused_nv(const FusedLaunch& fl, cudaStream_t s) {
+    // the dynamic shared-memory attribute is set by fused_blocks_per_sm before the first launch
+    k_fused_strands<N, VPL><<<fl.blocks, fl.warpsPerBlock * 32, fused_smem_for(N), s>>>(fl.objs, fl.items, fl.numItems);
+    return cudaGetLastError();
+}
+
+bool fused_config_valid(int n, int vpl) {
+    if (vpl < 1 || n % vpl != 0) return false;
+    const int L = n / vpl;
+    if (L > 32 || 32 % L != 0 || L < 2) return false;
+    if (vpl > 1 && (vpl % 2) != 0) return false;
+    return vpl <= 4;
+}
+
+int fused_smem_bytes(int n, int, int) { return fused_smem_for(n); }
+
+#define TFX_FUSED_CASE(NN, VV) \
+    if (fl.n == NN && fl.vpl == VV) return launch_fused_nv<NN, VV>(fl, s);
+
+cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s) {
+    TFX_FUSED_CASE(4, 1)
+    TFX_FUSED_CASE(4, 2)
+    TFX_FUSED_CASE(8, 1)
+    TFX_FUSED_CASE(8, 2)
+    TFX_FUSED_CASE(8, 4)
+    TFX_FUSED_CASE(16, 1)
+    TFX_FUSED_CASE(16, 2)
+    TFX_FUSED_CASE(16, 4)
+    TFX_FUSED_CASE(32, 1)
+    TFX_FUSED_CASE(32, 2)
+    TFX_FUSED_CASE(32, 4)
+    TFX_FUSED_CASE(64, 2)
+    TFX_FUSED_CASE(64, 4)
+    return cudaErrorInvalidValue;
+}
+
+#define TFX_FUSED_OCC(NN, VV)                                                                                     \
+    if (n == NN && vpl == VV) {                                                                                   \
+        int nb = 0;                                                                                               \
+        cudaError_t e = cudaFuncSetAttribute(k_fused_strands<NN, VV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                             fused_smem_for(NN));                                                 \
+        if (e != cudaSuccess) return 0;                                                                           \
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused_strands<NN, VV>, warps * 32, fused_smem_for(NN)); \
+        return nb;                                                                                                \
+    }
+
+int fused_blocks_per_sm(int n, int vpl, int warps) {
+    TFX_FUSED_OCC(4, 1)
+    TFX_FUSED_OCC(4, 2)
+    TFX_FUSED_OCC(8, 1)
+    TFX_FUSED_OCC(8, 2)
+    TFX_FUSED_OCC(8, 4)
+    TFX_FUSED_OCC(16, 1)
+    TFX_FUSED_OCC(16, 2)
+    TFX_FUSED_OCC(16, 4)
+    TFX_FUSED_OCC(32, 1)
+    TFX_FUSED_OCC(32, 2)
+    TFX_FUSED_OCC(32, 4)
+    TFX_FUSED_OCC(64, 2)
+    TFX_FUSED_OCC(64, 4)
+    return 0;
+}
+
+cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s) {
+    if (totalVerts <= 0) return cudaSuccess;
+    k_batch_mesh_skin<<<(totalVerts + 255) / 256, 256, 0, s>>>(meshes, nmeshes, totalVerts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_sdf(const SdfBatchLaunch& L, cudaStream_t s) {
+    if (L.nsdf <= 0) return cudaSuccess;
+    const long long q = L.totalQuads;
+    const unsigned gq = (unsigned)std::min<long long>((q + 255) / 256, 152LL * 32);
+    k_batch_sdf_init<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
+    if (L.totalTris > 0) {
+        const int warpsPerBlock = L.constructThreads / 32;
+        const long long blocks = (L.totalTris + warpsPerBlock - 1) / warpsPerBlock;
+        k_batch_sdf_construct<<<(unsigned)std::min<long long>(blocks, 152LL * 64), L.constructThreads, 0, s>>>(
+            L.sdfs, L.nsdf, L.totalTris);
+    }
+    k_batch_sdf_finalize<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
+    return cudaGetLastError();
+}
+
+}  // namespace tfx

@@ -5,25 +5,22 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <limits>
 #include <new>
-#include <string>
-#include <vector>
 
-#include "../../include/tressfx_gb300.h"
-#include "tfx_internal.h"
+#include "tfx_handles.h"
 
 using namespace tfx;
 
 // ============================================================================ errors
 static thread_local std::string g_last_error;
 
-static int fail(int code, const char* fmt, ...) {
+namespace tfx {
+int fail(int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -33,16 +30,47 @@ static int fail(int code, const char* fmt, ...) {
     return code;
 }
 
-static int cuda_fail(cudaError_t e, const char* what) {
+int cuda_fail(cudaError_t e, const char* what) {
     if (e == cudaErrorMemoryAllocation) return fail(TFX_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
     return fail(TFX_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define TFX_CUDA(call, what)                        \
-    do {                                            \
-        cudaError_t _e = (call);                    \
-        if (_e != cudaSuccess) return cuda_fail(_e, what); \
-    } while (0)
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+void context_retain(tfx_context c) { c->refs.fetch_add(1); }
+
+void context_release(tfx_context c) {
+    if (c->refs.fetch_sub(1) != 1) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto ev : c->stampEvents) cudaEventDestroy(ev);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+void fill_consts_header(DevSimConsts* c, const tfx_sim_params* p, int cpuLocalIterations) {
+    const float* w[4] = {p->wind, p->wind1, p->wind2, p->wind3};
+    for (int i = 0; i < 4; ++i) c->wind[i] = make_float4(w[i][0], w[i][1], w[i][2], w[i][3]);
+    c->damping = p->shape[0];
+    c->localStiffness = p->shape[1];
+    c->globalStiffness = p->shape[2];
+    c->globalRange = p->shape[3];
+    c->gravity = p->grav_time_tip[0];
+    c->timeStep = p->grav_time_tip[1];
+    c->tipSeparation = p->grav_time_tip[2];
+    // exp(-dampingCoeff * g_TimeStep * 60.0f), TressFXSimulation.hlsl:444, once per upload
+    const float arg = (-c->damping * c->timeStep) * 60.0f;
+    c->decay = std::exp(arg);
+    c->lengthIterations = p->sim_ints[0];
+    c->localIterations = p->sim_ints[1];
+    c->anyWind = (p->wind[0] != 0.0f || p->wind[1] != 0.0f || p->wind[2] != 0.0f) ? 1 : 0;
+    c->reserved0 = cpuLocalIterations;
+    c->vspCoeff = p->vsp[0];
+    c->vspAccelThreshold = p->vsp[1];
+    c->reset = p->reset_positions;
+    c->clamp = p->clamp_position_delta;
+}
+}  // namespace tfx
 
 extern "C" const char* tfx_status_string(int s) {
     switch (s) {
@@ -64,28 +92,6 @@ extern "C" const char* tfx_last_error(void) { return g_last_error.c_str(); }
 extern "C" int tfx_abi_version(void) { return TFX_ABI_VERSION; }
 
 // ============================================================================ context
-// A context is reference counted: every hair object, SDF and mesh created on it holds a reference,
-// so tfx_context_destroy may be called before the objects are destroyed; the stream is released
-// with the last reference.
-struct tfx_context_t {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::atomic<int> refs{1};
-    std::vector<std::string> stampNames;
-    std::vector<cudaEvent_t> stampEvents;
-};
-
-static void context_retain(tfx_context c) { c->refs.fetch_add(1); }
-
-static void context_release(tfx_context c) {
-    if (c->refs.fetch_sub(1) != 1) return;
-    cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    for (auto ev : c->stampEvents) cudaEventDestroy(ev);
-    cudaStreamDestroy(c->stream);
-    delete c;
-}
-
 extern "C" int tfx_context_create(int device, tfx_context* out) {
     if (!out) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_context_create: out is null");
     *out = nullptr;
@@ -102,6 +108,7 @@ extern "C" int tfx_context_create(int device, tfx_context* out) {
     auto* c = new (std::nothrow) tfx_context_t();
     if (!c) return fail(TFX_ERR_OUT_OF_MEMORY, "tfx_context_create: host allocation");
     c->device = device;
+    c->numSMs = prop.multiProcessorCount;
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreateWithFlags"); }
     *out = c;
@@ -164,28 +171,13 @@ extern "C" int tfx_host_free(void* p) {
 }
 
 // ============================================================================ hair object
-struct tfx_hair_t {
-    tfx_context ctx = nullptr;
-    int G = 0, n = 0, F = 0;
-    int64_t Vtot = 0, Stot = 0;
-    void* arena = nullptr;
-    size_t arenaBytes = 0;
-    HairView view{};
-    DevSimConsts* consts = nullptr;             // device
-    DevSimConsts* staging[2] = {nullptr, nullptr};  // pinned host (double buffered like m_SimCB[2])
-    cudaEvent_t stagingDone[2] = {nullptr, nullptr};
-    bool stagingUsed[2] = {false, false};
-    int stagingNext = 0;
-    struct Buf { void* ptr; size_t bytes; } bufs[10]{};
-};
-
-static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
 static bool valid_n(int n) { return n == 4 || n == 8 || n == 16 || n == 32 || n == 64; }
 
 // Bone indices / weights exactly as ApplyVertexBoneSkinning reads them (TressFXSimulation.hlsl:552-564):
 // index 0 always, index i>0 only when its weight is > 0; the divisor is w0 + sum(w_i > 0).
-static int validate_skinning(const float* skin, int64_t count, int64_t stride_items, const char* who) {
+// *maxBone receives the highest index read.
+static int validate_skinning(const float* skin, int64_t count, int64_t stride_items, const char* who, int* maxBone) {
+    int mb = 0;
     for (int64_t s = 0; s < count; ++s) {
         const float* idx = skin + 8 * s * stride_items;
         const float* w = idx + 4;
@@ -196,15 +188,17 @@ static int validate_skinning(const float* skin, int64_t count, int64_t stride_it
             if (!(idx[i] >= 0.0f) || !(idx[i] < (float)TFX_MAX_BONES))
                 return fail(TFX_ERR_BONE_INDEX, "%s: item %lld bone index %g outside [0, %d)", who, (long long)s * stride_items,
                             (double)idx[i], TFX_MAX_BONES);
+            mb = std::max(mb, (int)idx[i]);
             if (i > 0) wsum = wsum + w[i];
         }
         if (!(wsum > 0.0f) || !std::isfinite(wsum))
             return fail(TFX_ERR_BONE_WEIGHTS, "%s: item %lld bone weights sum to %g", who, (long long)s * stride_items, (double)wsum);
     }
+    if (maxBone) *maxBone = mb;
     return TFX_OK;
 }
 
-static int validate_desc(const tfx_hair_desc* d, const float* bone_skinning, const char* who) {
+static int validate_desc(const tfx_hair_desc* d, const float* bone_skinning, const char* who, int* maxBone) {
     if (!d || !bone_skinning) return fail(TFX_ERR_INVALID_ARGUMENT, "%s: null descriptor or skinning", who);
     if (!valid_n(d->verts_per_strand))
         return fail(TFX_ERR_VERTS_PER_STRAND, "%s: %d vertices per strand; must be 4, 8, 16, 32 or 64", who, d->verts_per_strand);
@@ -215,11 +209,21 @@ static int validate_desc(const tfx_hair_desc* d, const float* bone_skinning, con
     const int64_t Stot = G * (F + 1), Vtot = Stot * n;
     if (Vtot > (int64_t)std::numeric_limits<int32_t>::max() / 2 || 3 * Stot > (int64_t)std::numeric_limits<int32_t>::max())
         return fail(TFX_ERR_SIZE, "%s: %lld vertices exceed the 31-bit index space", who, (long long)Vtot);
-    return validate_skinning(bone_skinning, G, F + 1, who);
+    return validate_skinning(bone_skinning, G, F + 1, who, maxBone);
 }
 
 extern "C" int tfx_hair_validate(const tfx_hair_desc* d, const float* bone_skinning) {
-    return validate_desc(d, bone_skinning, "tfx_hair_validate");
+    return validate_desc(d, bone_skinning, "tfx_hair_validate", nullptr);
+}
+
+static void hair_free(tfx_hair h) {
+    if (h->arena) cudaFree(h->arena);
+    for (int i = 0; i < 2; ++i) {
+        if (h->staging[i]) cudaFreeHost(h->staging[i]);
+        if (h->stagingDone[i]) cudaEventDestroy(h->stagingDone[i]);
+    }
+    if (h->ctx) context_release(h->ctx);
+    delete h;
 }
 
 extern "C" int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* d, const float* positions, const float* tangents,
@@ -229,14 +233,15 @@ extern "C" int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* d, const fl
     *out = nullptr;
     if (!ctx || !d || !positions || !rest_lengths || !bone_skinning)
         return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_hair_create: null context, descriptor, positions, rest lengths or skinning");
-    if (int r = validate_desc(d, bone_skinning, "tfx_hair_create")) return r;
+    int maxBone = 0;
+    if (int r = validate_desc(d, bone_skinning, "tfx_hair_create", &maxBone)) return r;
     const int64_t G = d->num_guide_strands, n = d->verts_per_strand, F = d->follow_hairs_per_guide;
     const int64_t Stot = G * (F + 1), Vtot = Stot * n;
 
     TFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     auto* h = new (std::nothrow) tfx_hair_t();
     if (!h) return fail(TFX_ERR_OUT_OF_MEMORY, "tfx_hair_create: host allocation");
-    h->ctx = ctx; h->G = (int)G; h->n = (int)n; h->F = (int)F; h->Vtot = Vtot; h->Stot = Stot;
+    h->ctx = ctx; h->G = (int)G; h->n = (int)n; h->F = (int)F; h->Vtot = Vtot; h->Stot = Stot; h->maxBone = maxBone;
     context_retain(ctx);
 
     const size_t v16 = 16 * (size_t)Vtot, s16 = 16 * (size_t)Stot;
@@ -247,42 +252,29 @@ extern "C" int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* d, const fl
     offs[10] = total;
     total += align256(sizeof(DevSimConsts));
 
-    auto cleanup = [&]() {
-        if (h->arena) cudaFree(h->arena);
-        for (int i = 0; i < 2; ++i) {
-            if (h->staging[i]) cudaFreeHost(h->staging[i]);
-            if (h->stagingDone[i]) cudaEventDestroy(h->stagingDone[i]);
-        }
-        context_release(h->ctx);
-        delete h;
-    };
     cudaError_t e = cudaMalloc(&h->arena, total);
-    if (e != cudaSuccess) { h->arena = nullptr; cleanup(); return cuda_fail(e, "tfx_hair_create: cudaMalloc"); }
+    if (e != cudaSuccess) { h->arena = nullptr; hair_free(h); return cuda_fail(e, "tfx_hair_create: cudaMalloc"); }
     h->arenaBytes = total;
     char* base = (char*)h->arena;
     for (int b = 1; b <= 9; ++b) h->bufs[b] = {base + offs[b], sizes[b]};
     h->consts = (DevSimConsts*)(base + offs[10]);
     for (int i = 0; i < 2; ++i) {
         e = cudaMallocHost((void**)&h->staging[i], sizeof(DevSimConsts));
-        if (e != cudaSuccess) { h->staging[i] = nullptr; cleanup(); return cuda_fail(e, "tfx_hair_create: cudaMallocHost"); }
+        if (e != cudaSuccess) { h->staging[i] = nullptr; hair_free(h); return cuda_fail(e, "tfx_hair_create: cudaMallocHost"); }
         std::memset(h->staging[i], 0, sizeof(DevSimConsts));
         e = cudaEventCreateWithFlags(&h->stagingDone[i], cudaEventDisableTiming);
-        if (e != cudaSuccess) { h->stagingDone[i] = nullptr; cleanup(); return cuda_fail(e, "cudaEventCreate"); }
+        if (e != cudaSuccess) { h->stagingDone[i] = nullptr; hair_free(h); return cuda_fail(e, "cudaEventCreate"); }
     }
     cudaStream_t s = ctx->stream;
     // UploadGPUData (TressFXHairObject.cpp:528-558): Pos, Tan, Prev and PrevPrev from the asset;
     // InitialPosition / RestLength / RootOffset / SkinningData SRVs (:116-120).
-    const void* src[10] = {nullptr, positions, positions, positions, tangents, nullptr, positions, rest_lengths, follow_root_offsets,
-                           nullptr};
+    const void* src[10] = {nullptr, positions, positions, positions, tangents, nullptr, positions, rest_lengths,
+                           follow_root_offsets, bone_skinning};
     e = cudaMemsetAsync(h->arena, 0, total, s);
-    for (int b = 1; b <= 8 && e == cudaSuccess; ++b)
+    for (int b = 1; b <= 9 && e == cudaSuccess; ++b)
         if (src[b]) e = cudaMemcpyAsync(h->bufs[b].ptr, src[b], sizes[b], cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) {
-        // skinning data is per strand; the reference fills only guide strands (TressFXAsset.cpp:471-477)
-        e = cudaMemcpyAsync(h->bufs[9].ptr, bone_skinning, sizes[9], cudaMemcpyHostToDevice, s);
-    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "tfx_hair_create: upload"); }
+    if (e != cudaSuccess) { hair_free(h); return cuda_fail(e, "tfx_hair_create: upload"); }
 
     HairView& v = h->view;
     v.pos = (float4*)h->bufs[TFX_BUF_POSITIONS].ptr;
@@ -304,13 +296,7 @@ extern "C" int tfx_hair_destroy(tfx_hair h) {
     if (!h) return TFX_OK;
     cudaSetDevice(h->ctx->device);
     cudaStreamSynchronize(h->ctx->stream);
-    cudaFree(h->arena);
-    for (int i = 0; i < 2; ++i) {
-        cudaFreeHost(h->staging[i]);
-        cudaEventDestroy(h->stagingDone[i]);
-    }
-    context_release(h->ctx);
-    delete h;
+    hair_free(h);
     return TFX_OK;
 }
 
@@ -325,26 +311,7 @@ extern "C" int tfx_hair_update_constants(tfx_hair h, const tfx_sim_params* p, in
     h->stagingNext ^= 1;
     if (h->stagingUsed[slot]) TFX_CUDA(cudaEventSynchronize(h->stagingDone[slot]), "cudaEventSynchronize");
     DevSimConsts* c = h->staging[slot];
-    const float* w[4] = {p->wind, p->wind1, p->wind2, p->wind3};
-    for (int i = 0; i < 4; ++i) c->wind[i] = make_float4(w[i][0], w[i][1], w[i][2], w[i][3]);
-    c->damping = p->shape[0];
-    c->localStiffness = p->shape[1];
-    c->globalStiffness = p->shape[2];
-    c->globalRange = p->shape[3];
-    c->gravity = p->grav_time_tip[0];
-    c->timeStep = p->grav_time_tip[1];
-    c->tipSeparation = p->grav_time_tip[2];
-    // exp(-dampingCoeff * g_TimeStep * 60.0f), TressFXSimulation.hlsl:444, once per upload
-    const float arg = (-c->damping * c->timeStep) * 60.0f;
-    c->decay = std::exp(arg);
-    c->lengthIterations = p->sim_ints[0];
-    c->localIterations = p->sim_ints[1];
-    c->anyWind = (p->wind[0] != 0.0f || p->wind[1] != 0.0f || p->wind[2] != 0.0f) ? 1 : 0;
-    c->reserved0 = 0;
-    c->vspCoeff = p->vsp[0];
-    c->vspAccelThreshold = p->vsp[1];
-    c->reset = p->reset_positions;
-    c->clamp = p->clamp_position_delta;
+    fill_consts_header(c, p, 0);
     std::memcpy(c->bones, p->bone_matrices, (size_t)num_bones * 64);
     const size_t bytes = offsetof(DevSimConsts, bones) + (size_t)num_bones * 64;
     TFX_CUDA(cudaSetDevice(h->ctx->device), "cudaSetDevice");
@@ -408,6 +375,8 @@ extern "C" int tfx_hair_read_async(tfx_hair h, int b, void* dst, size_t bytes) {
 extern "C" int tfx_hair_write_async(tfx_hair h, int b, const void* srcp, size_t bytes) {
     if (int r = hair_buf(h, b, bytes, "tfx_hair_write")) return r;
     if (!srcp && bytes) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_hair_write: null source");
+    if (b == TFX_BUF_BONE_SKINNING)
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_hair_write: the skinning buffer is fixed at creation (validated there)");
     TFX_CUDA(cudaSetDevice(h->ctx->device), "cudaSetDevice");
     TFX_CUDA(cudaMemcpyAsync(h->bufs[b].ptr, srcp, bytes, cudaMemcpyHostToDevice, h->ctx->stream), "tfx_hair_write: copy");
     return TFX_OK;
@@ -435,16 +404,6 @@ extern "C" int tfx_hair_get_counts(tfx_hair h, int32_t out[4]) {
 }
 
 // ============================================================================ SDF
-struct tfx_sdf_t {
-    tfx_context ctx = nullptr;
-    uint32_t* grid = nullptr;
-    int64_t alloc = 0;
-    const float4* mesh = nullptr;
-    int nverts = 0;
-    const uint32_t* idx = nullptr;
-    int ntri = 0;
-};
-
 extern "C" int tfx_sdf_create(tfx_context ctx, int64_t alloc_cells, tfx_sdf* out) {
     if (!out) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_sdf_create: out is null");
     *out = nullptr;
@@ -559,21 +518,6 @@ extern "C" int tfx_sdf_get_buffer(tfx_sdf s, void** ptr, size_t* bytes) {
 }
 
 // ============================================================================ collision mesh
-struct tfx_mesh_t {
-    tfx_context ctx = nullptr;
-    int nverts = 0, ntri = 0;
-    void* arena = nullptr;
-    float4* bind = nullptr;     // {position, normal}[nverts]
-    float4* skinned = nullptr;  // {position, normal}[nverts]
-    float4* skin = nullptr;     // {boneIndex, boneWeight}[nverts]
-    uint32_t* idx = nullptr;
-    float4* bones = nullptr;    // 512 matrices
-    float* staging[2] = {nullptr, nullptr};
-    cudaEvent_t stagingDone[2] = {nullptr, nullptr};
-    bool stagingUsed[2] = {false, false};
-    int stagingNext = 0;
-};
-
 extern "C" int tfx_mesh_destroy(tfx_mesh m) {
     if (!m) return TFX_OK;
     cudaSetDevice(m->ctx->device);
@@ -597,11 +541,12 @@ extern "C" int tfx_mesh_create(tfx_context ctx, const float* vertices, int nvert
     for (int64_t i = 0; i < 3 * (int64_t)ntri; ++i)
         if (indices[i] >= (uint32_t)nverts)
             return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_mesh_create: index %u at %lld >= %d vertices", indices[i], (long long)i, nverts);
-    if (int r = validate_skinning(skinning, nverts, 1, "tfx_mesh_create")) return r;
+    int maxBone = 0;
+    if (int r = validate_skinning(skinning, nverts, 1, "tfx_mesh_create", &maxBone)) return r;
     TFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     auto* m = new (std::nothrow) tfx_mesh_t();
     if (!m) return fail(TFX_ERR_OUT_OF_MEMORY, "tfx_mesh_create: host allocation");
-    m->ctx = ctx; m->nverts = nverts; m->ntri = ntri;
+    m->ctx = ctx; m->nverts = nverts; m->ntri = ntri; m->maxBone = maxBone;
     context_retain(ctx);
     const size_t vb = 32 * (size_t)nverts, ib = 12 * (size_t)ntri, bb = 64 * (size_t)TFX_MAX_BONES;
     const size_t total = 3 * align256(vb) + align256(ib) + align256(bb);

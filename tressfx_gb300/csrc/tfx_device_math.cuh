@@ -147,4 +147,37 @@ __device__ __forceinline__ float3 xform_row(float3 p, float w, const float (&m)[
                ((p.x * m[0][2] + p.y * m[1][2]) + p.z * m[2][2]) + w * m[3][2]);
 }
 
+struct DC { float4 p0, p1; };
+
+// ApplyDistanceConstraint + ConstraintMultiplier, TressFXSimulation.hlsl:214-230, :377-387 (stiffness 1).
+__device__ __forceinline__ DC distance_constraint(float4 p0, float4 p1, float target) {
+    float3 delta = sub(xyz(p1), xyz(p0));
+    const float distance = fmaxf(length(delta), 1e-7f);
+    const float stretching = 1.0f - target / distance;
+    delta = mul(stretching, delta);
+    float m0, m1;
+    if (p0.w > 0.0f) { if (p1.w > 0.0f) { m0 = 0.5f; m1 = 0.5f; } else { m0 = 1.0f; m1 = 0.0f; } }
+    else { if (p1.w > 0.0f) { m0 = 0.0f; m1 = 1.0f; } else { m0 = 0.0f; m1 = 0.0f; } }
+    const float3 a = mul(mul(m0, delta), 1.0f);
+    const float3 b = mul(mul(m1, delta), 1.0f);
+    p0.x = p0.x + a.x; p0.y = p0.y + a.y; p0.z = p0.z + a.z;
+    p1.x = p1.x - b.x; p1.y = p1.y - b.y; p1.z = p1.z - b.z;
+    return DC{p0, p1};
+}
+
+static constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ float4 shfl4(float4 v, int src) {
+    return make_float4(__shfl_sync(FULL, v.x, src), __shfl_sync(FULL, v.y, src), __shfl_sync(FULL, v.z, src),
+                       __shfl_sync(FULL, v.w, src));
+}
+__device__ __forceinline__ float4 shfl4_down(float4 v, int d) {
+    return make_float4(__shfl_down_sync(FULL, v.x, d), __shfl_down_sync(FULL, v.y, d), __shfl_down_sync(FULL, v.z, d),
+                       __shfl_down_sync(FULL, v.w, d));
+}
+__device__ __forceinline__ float4 shfl4_up(float4 v, int d) {
+    return make_float4(__shfl_up_sync(FULL, v.x, d), __shfl_up_sync(FULL, v.y, d), __shfl_up_sync(FULL, v.z, d),
+                       __shfl_up_sync(FULL, v.w, d));
+}
+
 }  // namespace tfx

@@ -5,68 +5,9 @@
 // over the encoding = min |d|, ties to the positive value) and plain floats after Finalize.
 // atomicMin is order independent, and the distance arithmetic below is the reference's in the
 // same order with no FMA contraction, so the finished grid matches the oracle bit for bit.
-#include "tfx_device_math.cuh"
-#include "tfx_internal.h"
+#include "tfx_sdf_math.cuh"
 
 namespace tfx {
-
-// FloatFlip3 / IFloatFlip3, TressFXSDFCollision.hlsl:92-100
-__device__ __forceinline__ uint32_t float_flip3(float f) {
-    const uint32_t u = __float_as_uint(f);
-    return (u << 1) | (u >> 31);
-}
-__device__ __forceinline__ uint32_t ifloat_flip3(uint32_t u) { return (u >> 1) | (u << 31); }
-
-// GetSdfCoordinates, :103-113
-__device__ __forceinline__ int3 sdf_coords(const SdfGrid& g, float3 p) {
-    const float sx = (p.x - g.ox) / g.cell, sy = (p.y - g.oy) / g.cell, sz = (p.z - g.oz) / g.cell;
-    return make_int3(ftoi(sx), ftoi(sy), ftoi(sz));
-}
-// GetSdfCellPosition, :115-121
-__device__ __forceinline__ float3 sdf_cell_pos(const SdfGrid& g, int x, int y, int z) {
-    const float3 c = mk3((float)x * g.cell, (float)y * g.cell, (float)z * g.cell);
-    return add(c, mk3(g.ox, g.oy, g.oz));
-}
-
-// DistancePointToEdge, :147-159 (only the distance reaches the result)
-__device__ __forceinline__ float dist_point_edge(float3 p, float3 x0, float3 x1) {
-    const float3 x10 = sub(x1, x0);
-    float t = dot(sub(x1, p), x10) / dot(x10, x10);
-    t = fmaxf(0.0f, fminf(t, 1.0f));
-    const float3 a = sub(p, add(mul(t, x0), mul(1.0f - t, x1)));
-    return length(a);
-}
-
-// SignedDistancePointToTriangle, :163-215
-__device__ __forceinline__ float signed_dist_triangle(float3 p, float3 x0, float3 x1, float3 x2) {
-    float d;
-    float3 x02 = sub(x0, x2);
-    const float l0 = length(x02) + 1e-30f;
-    x02 = divs(x02, l0);
-    float3 x12 = sub(x1, x2);
-    const float l1 = dot(x12, x02);
-    x12 = sub(x12, mul(l1, x02));
-    const float l2 = length(x12) + 1e-30f;
-    x12 = divs(x12, l2);
-    const float3 px2 = sub(p, x2);
-    const float b = dot(x12, px2) / l2;
-    const float a = (dot(x02, px2) - l1 * b) / l0;
-    const float c = (1.0f - a) - b;
-    const float3 nTri = cross(sub(x1, x0), sub(x2, x0));
-    const float tol = 1e-8f;
-    if (a >= -tol && b >= -tol && c >= -tol) {
-        const float3 nn = sub(p, add(add(mul(a, x0), mul(b, x1)), mul(c, x2)));
-        d = length(nn);
-    } else {
-        d = dist_point_edge(p, x0, x1);
-        const float d12 = dist_point_edge(p, x1, x2);
-        const float d02 = dist_point_edge(p, x0, x2);
-        d = fminf(d, d12);
-        d = fminf(d, d02);
-    }
-    d = (dot(sub(p, x0), nTri) < 0.0f) ? -d : d;
-    return d;
-}
 
 // --------------------------------------------------------------------------------------------
 // InitializeSignedDistanceField, :301-312 (vectorised: 4 cells per 16 B store)
@@ -114,34 +55,6 @@ __global__ void __launch_bounds__(256) k_sdf_finalize(uint32_t* __restrict__ sdf
     }
     for (long long i = (n4 << 2) + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells; i += stride)
         sdf[i] = ifloat_flip3(sdf[i]);
-}
-
-// GetSignedDistance + TrilinearInterpolate, :414-527
-__device__ __forceinline__ float lerp_ref(float a, float b, float t) { return a * (1.0f - t) + b * t; }
-
-__device__ __forceinline__ float sdf_lookup(const float* __restrict__ sdf, const SdfGrid& g, float3 p) {
-    const int3 gc = sdf_coords(g, p);
-    if (!(0 <= gc.x && gc.x < g.nx - 2) || !(0 <= gc.y && gc.y < g.ny - 2) || !(0 <= gc.z && gc.z < g.nz - 2))
-        return 1e10f;
-    const long long X = 1, Y = g.nx, Z = (long long)g.ny * g.nx;
-    const long long base = Z * gc.z + Y * gc.y + gc.x;
-    float d[8];
-    d[0] = __ldg(sdf + base);
-    d[1] = __ldg(sdf + base + X);
-    d[2] = __ldg(sdf + base + Y);
-    d[3] = __ldg(sdf + base + Y + X);
-    d[4] = __ldg(sdf + base + Z);
-    d[5] = __ldg(sdf + base + Z + X);
-    d[6] = __ldg(sdf + base + Z + Y);
-    d[7] = __ldg(sdf + base + Z + Y + X);
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-        if (d[j] == 1e10f) return 1e10f;
-    const float3 cp = sdf_cell_pos(g, gc.x, gc.y, gc.z);
-    const float3 ip = divs(sub(p, cp), g.cell);
-    const float b0 = lerp_ref(lerp_ref(d[0], d[1], ip.x), lerp_ref(d[2], d[3], ip.x), ip.y);
-    const float b1 = lerp_ref(lerp_ref(d[4], d[5], ip.x), lerp_ref(d[6], d[7], ip.x), ip.y);
-    return lerp_ref(b0, b1, ip.z);
 }
 
 // CollideHairVerticesWithSdf_forward, :531-595.  One thread per hair vertex (guides and follows).

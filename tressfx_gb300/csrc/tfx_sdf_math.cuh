@@ -1,0 +1,186 @@
+// Device-side SDF helpers shared by the plain SDF kernels and the batched (tiled) build / fused
+// collide: FloatFlip3 encoding, grid coordinates, signed point-triangle distance and the
+// trilinear lookup of src/Shaders/TressFXSDFCollision.hlsl, evaluated in the reference's order.
+#pragma once
+#include "tfx_device_math.cuh"
+#include "tfx_internal.h"
+
+namespace tfx {
+
+// FloatFlip3 / IFloatFlip3, TressFXSDFCollision.hlsl:92-100
+__device__ __forceinline__ uint32_t float_flip3(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u << 1) | (u >> 31);
+}
+__device__ __forceinline__ uint32_t ifloat_flip3(uint32_t u) { return (u >> 1) | (u << 31); }
+
+// GetSdfCoordinates, :103-113
+__device__ __forceinline__ int3 sdf_coords(const SdfGrid& g, float3 p) {
+    const float sx = (p.x - g.ox) / g.cell, sy = (p.y - g.oy) / g.cell, sz = (p.z - g.oz) / g.cell;
+    return make_int3(ftoi(sx), ftoi(sy), ftoi(sz));
+}
+// GetSdfCellPosition, :115-121
+__device__ __forceinline__ float3 sdf_cell_pos(const SdfGrid& g, int x, int y, int z) {
+    const float3 c = mk3((float)x * g.cell, (float)y * g.cell, (float)z * g.cell);
+    return add(c, mk3(g.ox, g.oy, g.oz));
+}
+
+// DistancePointToEdge, :147-159 (only the distance reaches the result)
+__device__ __forceinline__ float dist_point_edge(float3 p, float3 x0, float3 x1) {
+    const float3 x10 = sub(x1, x0);
+    float t = dot(sub(x1, p), x10) / dot(x10, x10);
+    t = fmaxf(0.0f, fminf(t, 1.0f));
+    const float3 a = sub(p, add(mul(t, x0), mul(1.0f - t, x1)));
+    return length(a);
+}
+
+// SignedDistancePointToTriangle, :163-215
+__device__ __forceinline__ float signed_dist_triangle(float3 p, float3 x0, float3 x1, float3 x2) {
+    float d;
+    float3 x02 = sub(x0, x2);
+    const float l0 = length(x02) + 1e-30f;
+    x02 = divs(x02, l0);
+    float3 x12 = sub(x1, x2);
+    const float l1 = dot(x12, x02);
+    x12 = sub(x12, mul(l1, x02));
+    const float l2 = length(x12) + 1e-30f;
+    x12 = divs(x12, l2);
+    const float3 px2 = sub(p, x2);
+    const float b = dot(x12, px2) / l2;
+    const float a = (dot(x02, px2) - l1 * b) / l0;
+    const float c = (1.0f - a) - b;
+    const float3 nTri = cross(sub(x1, x0), sub(x2, x0));
+    const float tol = 1e-8f;
+    if (a >= -tol && b >= -tol && c >= -tol) {
+        const float3 nn = sub(p, add(add(mul(a, x0), mul(b, x1)), mul(c, x2)));
+        d = length(nn);
+    } else {
+        d = dist_point_edge(p, x0, x1);
+        const float d12 = dist_point_edge(p, x1, x2);
+        const float d02 = dist_point_edge(p, x0, x2);
+        d = fminf(d, d12);
+        d = fminf(d, d02);
+    }
+    d = (dot(sub(p, x0), nTri) < 0.0f) ? -d : d;
+    return d;
+}
+
+// The triangle-only terms of SignedDistancePointToTriangle / DistancePointToEdge, computed once per
+// triangle; signed_dist_pre(p, T) then does the per-cell part.  Every term is the same expression
+// on the same inputs as in signed_dist_triangle, so the distance is bit-identical.
+struct TriPre {
+    float3 x0, x1, x2;
+    float3 x02n, x12n;   // normalised edge frame
+    float l0, l1, l2;
+    float3 nTri;
+    float3 e01, e12, e02; // x1-x0, x2-x1, x2-x0 (the x10 of the three edge calls)
+    float d01, d12, d02;  // dot(x10, x10) of the three edge calls
+};
+
+__device__ __forceinline__ TriPre tri_pre(float3 x0, float3 x1, float3 x2) {
+    TriPre T;
+    T.x0 = x0; T.x1 = x1; T.x2 = x2;
+    float3 x02 = sub(x0, x2);
+    T.l0 = length(x02) + 1e-30f;
+    T.x02n = divs(x02, T.l0);
+    float3 x12 = sub(x1, x2);
+    T.l1 = dot(x12, T.x02n);
+    x12 = sub(x12, mul(T.l1, T.x02n));
+    T.l2 = length(x12) + 1e-30f;
+    T.x12n = divs(x12, T.l2);
+    T.nTri = cross(sub(x1, x0), sub(x2, x0));
+    T.e01 = sub(x1, x0); T.d01 = dot(T.e01, T.e01);
+    T.e12 = sub(x2, x1); T.d12 = dot(T.e12, T.e12);
+    T.e02 = sub(x2, x0); T.d02 = dot(T.e02, T.e02);
+    return T;
+}
+
+// DistancePointToEdge(p, a, b) with x10 = b - a and dot(x10, x10) precomputed.
+__device__ __forceinline__ float dist_point_edge_pre(float3 p, float3 a, float3 b, float3 x10, float dd) {
+    float t = dot(sub(b, p), x10) / dd;
+    t = fmaxf(0.0f, fminf(t, 1.0f));
+    const float3 q = sub(p, add(mul(t, a), mul(1.0f - t, b)));
+    return length(q);
+}
+
+__device__ __forceinline__ float signed_dist_pre(float3 p, const TriPre& T) {
+    float d;
+    const float3 px2 = sub(p, T.x2);
+    const float b = dot(T.x12n, px2) / T.l2;
+    const float a = (dot(T.x02n, px2) - T.l1 * b) / T.l0;
+    const float c = (1.0f - a) - b;
+    const float tol = 1e-8f;
+    if (a >= -tol && b >= -tol && c >= -tol) {
+        const float3 nn = sub(p, add(add(mul(a, T.x0), mul(b, T.x1)), mul(c, T.x2)));
+        d = length(nn);
+    } else {
+        d = dist_point_edge_pre(p, T.x0, T.x1, T.e01, T.d01);
+        const float d12 = dist_point_edge_pre(p, T.x1, T.x2, T.e12, T.d12);
+        const float d02 = dist_point_edge_pre(p, T.x0, T.x2, T.e02, T.d02);
+        d = fminf(d, d12);
+        d = fminf(d, d02);
+    }
+    d = (dot(sub(p, T.x0), T.nTri) < 0.0f) ? -d : d;
+    return d;
+}
+
+// The cell box ConstructSignedDistanceField visits for a triangle (:351-363): AABB +- one cell,
+// grid coordinates -+ GRID_MARGIN, clamped to the grid.
+__device__ __forceinline__ void tri_cell_box(const SdfGrid& g, float3 t0, float3 t1, float3 t2, int3& lo, int3& hi) {
+    const float3 m = mk3(g.cell, g.cell, g.cell);
+    const float3 aabbMin = sub(vmin(t0, vmin(t1, t2)), m);
+    const float3 aabbMax = add(vmax(t0, vmax(t1, t2)), m);
+    lo = sdf_coords(g, aabbMin);
+    hi = sdf_coords(g, aabbMax);
+    lo.x = max(0, min(lo.x - 1, g.nx - 1)); lo.y = max(0, min(lo.y - 1, g.ny - 1)); lo.z = max(0, min(lo.z - 1, g.nz - 1));
+    hi.x = max(0, min(hi.x + 1, g.nx - 1)); hi.y = max(0, min(hi.y + 1, g.ny - 1)); hi.z = max(0, min(hi.z + 1, g.nz - 1));
+}
+
+// GetSignedDistance + TrilinearInterpolate, :414-527
+__device__ __forceinline__ float lerp_ref(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+__device__ __forceinline__ float sdf_lookup(const float* __restrict__ sdf, const SdfGrid& g, float3 p) {
+    const int3 gc = sdf_coords(g, p);
+    if (!(0 <= gc.x && gc.x < g.nx - 2) || !(0 <= gc.y && gc.y < g.ny - 2) || !(0 <= gc.z && gc.z < g.nz - 2))
+        return 1e10f;
+    const long long X = 1, Y = g.nx, Z = (long long)g.ny * g.nx;
+    const long long base = Z * gc.z + Y * gc.y + gc.x;
+    float d[8];
+    d[0] = __ldg(sdf + base);
+    d[1] = __ldg(sdf + base + X);
+    d[2] = __ldg(sdf + base + Y);
+    d[3] = __ldg(sdf + base + Y + X);
+    d[4] = __ldg(sdf + base + Z);
+    d[5] = __ldg(sdf + base + Z + X);
+    d[6] = __ldg(sdf + base + Z + Y);
+    d[7] = __ldg(sdf + base + Z + Y + X);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (d[j] == 1e10f) return 1e10f;
+    const float3 cp = sdf_cell_pos(g, gc.x, gc.y, gc.z);
+    const float3 ip = divs(sub(p, cp), g.cell);
+    const float b0 = lerp_ref(lerp_ref(d[0], d[1], ip.x), lerp_ref(d[2], d[3], ip.x), ip.y);
+    const float b1 = lerp_ref(lerp_ref(d[4], d[5], ip.x), lerp_ref(d[6], d[7], ip.x), ip.y);
+    return lerp_ref(b0, b1, ip.z);
+}
+
+// CollideHairVerticesWithSdf_forward for one vertex (j >= 2): returns true and the projected
+// position when the vertex is pushed out (then Pos.xyz and Prev.xyz both take it).
+__device__ __forceinline__ bool sdf_collide_point(const float* __restrict__ sdf, const SdfGrid& g, float margin, float3 p,
+                                                  float3& proj) {
+    const float distance = sdf_lookup(sdf, g, p);
+    if (distance > margin) return false;
+    const float h = 0.1f * g.cell;
+    const float fx = sdf_lookup(sdf, g, add(p, mul(mk3(1.0f, 0.0f, 0.0f), h)));
+    const float fy = sdf_lookup(sdf, g, add(p, mul(mk3(0.0f, 1.0f, 0.0f), h)));
+    const float fz = sdf_lookup(sdf, g, add(p, mul(mk3(0.0f, 0.0f, 1.0f), h)));
+    const float3 grad = mk3((fx - distance) / h, (fy - distance) / h, (fz - distance) / h);
+    const float3 nrm = normalize(grad);
+    if (distance < margin) {
+        proj = add(p, mul(nrm, margin - distance));
+        return true;
+    }
+    return false;
+}
+
+}  // namespace tfx

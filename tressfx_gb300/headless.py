@@ -104,3 +104,49 @@ class PlainPipeline:
         for x in self.hair + self.meshes + self.sdfs:
             if x is not None:
                 x.close()
+
+
+class BatchedPipeline(PlainPipeline):
+    """The same objects as PlainPipeline, advanced by the batched path: one graph launch per frame."""
+
+    def __init__(self, ctx: Context, scene: Scene, autotune_frames: int = 0):
+        from .api import Batch
+        super().__init__(ctx, scene)
+        self.batch = Batch(ctx)
+        self.sdf_index: list[int] = []
+        for m, s, o in zip(self.meshes, self.sdfs, scene.objects):
+            self.sdf_index.append(self.batch.add_sdf(s, m, o.sdf_dims) if s is not None else -1)
+        for h, si in zip(self.hair, self.sdf_index):
+            self.batch.add_hair(h, si)
+        self.batch.build()
+        self.autotune_frames = autotune_frames
+        self._tuned = autotune_frames <= 0
+
+    def set_inputs(self, fin: FrameInputs) -> None:
+        """Host side of a frame for the batch: constants, grids and mesh bones into the frame block."""
+        self.prepare(fin)
+        for i, h in enumerate(self.hair):
+            self.batch.set_hair_constants(i, h.current_params(), h.num_bones, h.cpu_local_iterations)
+        for i, (o, si, g, mb) in enumerate(zip(self.scene.objects, self.sdf_index, fin.grids, fin.mesh_bones)):
+            if si >= 0:
+                self.batch.set_sdf_frame(si, g, margin_world(o, g))
+                self.batch.set_mesh_bones(si, mb)
+
+    def run(self, fin: FrameInputs) -> None:
+        if not self._tuned:
+            self.batch.autotune(self.autotune_frames)
+            self._tuned = True
+        self.batch.run()
+        for h in self.hair:
+            h.increase_simulation_frame()
+        self.frame += 1
+
+    def step(self, frame: int | None = None) -> FrameInputs:
+        fin = FrameInputs(self.scene, self.frame if frame is None else frame)
+        self.set_inputs(fin)
+        self.run(fin)
+        return fin
+
+    def close(self) -> None:
+        self.batch.close()
+        super().close()

@@ -459,3 +459,56 @@ def sdf_grid_for(obj: SceneObject, bones: np.ndarray):
     g.cell_size = float(cell)
     g.num_cells_x, g.num_cells_y, g.num_cells_z = nx, ny, nz
     return g
+
+
+def scene_batched(seed: int = 4, num_objects: int = 64, min_strands: int = 512, max_strands: int = 50000,
+                  verts=(8, 16, 32, 64), min_tris: int = 5000, max_tris: int = 30000, sdf_choices=(32, 48, 64, 96, 128),
+                  follows: int = 0, frames: int = 300) -> Scene:
+    """Batched uneven workload: `num_objects` hair objects, strand counts log-uniform in
+    [min_strands, max_strands] padded to a multiple of 64 (the reference's asset rule), vertices per
+    strand drawn from `verts`, damping ~U(0.01, 0.1), stiffnesses ~U(0.1, 0.9), each object on its
+    own head mesh (triangles log-uniform in [min_tris, max_tris]) with its own SDF of 32^3..128^3
+    and its own nod/turn phase.  Objects sit on a 1 m grid so their SDFs do not overlap."""
+    rng = np.random.default_rng(seed)
+    objs = []
+    side = int(math.ceil(math.sqrt(num_objects)))
+    for k in range(num_objects):
+        G = int(math.exp(rng.uniform(math.log(min_strands), math.log(max_strands))))
+        G = max(64, ((G + 63) // 64) * 64)
+        n = int(rng.choice(verts))
+        tris = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
+        dims = int(rng.choice(sdf_choices))
+        cx, cz = (k % side) * 1.0, (k // side) * 1.0
+        center = (cx, 1.6, cz)
+        roots, normals = sample_on_ellipsoid(center, (0.1, 0.1, 0.1), G, rng, y_min=-0.2)
+        seg = 0.12 / n
+        guides = grow_strands(roots, normals, n, seg, 15.0, rng)
+        skin = np.zeros((G, 8), dtype=np.float32)
+        skin[:, 0:4] = (2, 0, 0, 0)
+        skin[:, 4:8] = (1, 0, 0, 0)
+        asset = build_asset(guides, follows, tip_separation=0.5, follow_radius=0.002, rng=rng, bone_skinning=skin)
+        st = _settings(damping=float(rng.uniform(0.01, 0.1)), local_constraint_stiffness=float(rng.uniform(0.1, 0.9)),
+                       global_constraint_stiffness=float(rng.uniform(0.1, 0.9)), global_constraints_range=0.3,
+                       local_constraints_iterations=2, length_constraints_iterations=2, gravity_magnitude=9.8,
+                       vsp_coeff=0.6, wind_magnitude=float(rng.uniform(0.0, 2.0)))
+        nl, nq = mesh_lat_lon_for(int(tris * 0.7))
+        hv, hi = ellipsoid_mesh(center, (0.1, 0.1, 0.1), nl, nq)
+        nl2, nq2 = mesh_lat_lon_for(int(tris * 0.3))
+        ev, ei = ellipsoid_mesh((cx, 1.5, cz + 0.015), (0.06, 0.09, 0.07), nl2, nq2)
+        hs = np.zeros((len(hv), 8), dtype=np.float32)
+        hs[:, 0:4] = (2, 0, 0, 0)
+        hs[:, 4] = 1.0
+        es = np.zeros((len(ev), 8), dtype=np.float32)
+        es[:, 0:4] = (1, 0, 0, 0)
+        es[:, 4] = 1.0
+        mesh = merge_meshes([(hv, hi, hs), (ev, ei, es)])
+        pivot = (cx, 1.48, cz)
+        phase = float(rng.uniform(0.0, 1.0))
+        base = nod_turn_bones(pivot, nod_deg=float(rng.uniform(10, 30)), turn_deg=float(rng.uniform(10, 40)))
+        bones = (lambda b, ph: (lambda t: b(t + ph)))(base, phase)
+        p = mesh.vertices[:, :3].astype(np.float64)
+        lo, hi_ = p.min(0), p.max(0)
+        extent = float((hi_ - lo).max()) + 2 * 0.02
+        objs.append(SceneObject(asset, st, bones, mesh, bones, (dims,) * 3, extent / dims, (lo + hi_) / 2, follow_bone=2))
+    sc = Scene(f"batched_{num_objects}obj", objs, frames=frames)
+    return sc
