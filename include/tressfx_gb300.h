@@ -234,6 +234,18 @@ int tfx_sdf_read(tfx_sdf sdf, void* host_dst, size_t bytes);
 int tfx_sdf_write(tfx_sdf sdf, const void* host_src, size_t bytes);
 int tfx_sdf_get_buffer(tfx_sdf sdf, void** device_ptr, size_t* bytes);
 
+/* Largest grid (X*Y*Z cells) that tfx_sdf_build_static accepts: 128^3, 8 MiB of scratch words. */
+#define TFX_SDF_STATIC_MAX_CELLS 2097152
+/* No counterpart in the reference.  Initialize + Construct + Finalize of `grid` from a DEVICE mesh
+ * ({float4 position, float4 normal}[num_vertices], uint32[3*num_triangles]) into the DEVICE float
+ * buffer sdf_out[X*Y*Z], the same grid tfx_sdf_update builds, without allocating anything: the
+ * FloatFlip3 build words live in one static device array per device (TFX_SDF_STATIC_MAX_CELLS
+ * words; larger grids return TFX_ERR_SIZE).  Nothing has to be zeroed first.  The first call on a
+ * device looks the array up (make it before any stream capture).  Calls that can overlap on one
+ * device (other contexts or streams) race on that array; calls on one context are stream-ordered. */
+int tfx_sdf_build_static(tfx_context ctx, const tfx_sdf_grid* grid, const void* mesh_vertices, int num_vertices,
+                         const uint32_t* indices, int num_triangles, float* sdf_out);
+
 /* ---------------------------------------------------------------------------------- collision mesh */
 /* TressFXBoneSkinning::Initialize (TressFXBoneSkinning.cpp:287-404): uploads the bind-pose mesh
  * {float4 position, float4 normal}[num_vertices], uint32[3*num_triangles] and per-vertex

@@ -159,6 +159,7 @@ _PROTOS = {
     "tfx_sdf_read": (C.c_int, [P, P, C.c_size_t]),
     "tfx_sdf_write": (C.c_int, [P, P, C.c_size_t]),
     "tfx_sdf_get_buffer": (C.c_int, [P, C.POINTER(P), C.POINTER(C.c_size_t)]),
+    "tfx_sdf_build_static": (C.c_int, [P, P, P, C.c_int, P, C.c_int, P]),
     "tfx_mesh_create": (C.c_int, [P, P, C.c_int, P, C.c_int, P, C.POINTER(P)]),
     "tfx_mesh_destroy": (C.c_int, [P]),
     "tfx_mesh_skin": (C.c_int, [P, P, C.c_int]),
