@@ -49,3 +49,20 @@ def test_build_targets_sm103a_with_exact_fp_flags():
     assert "-gencode=arch=compute_103a,code=sm_103a" in flags
     for f in ("-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"):
         assert f in flags
+
+
+def test_host_library_exports_the_reference_classes(built_lib):
+    """libtressfx_host.so carries the C++ host classes with the reference's method names."""
+    from tressfx_gb300 import build as B
+    assert B.HOST_LIB_PATH.exists()
+    out = subprocess.run(["nm", "-DC", "--defined-only", str(B.HOST_LIB_PATH)], capture_output=True, text=True).stdout
+    for sym in ("TressFXHairObject::TressFXHairObject(TressFXAsset*, EI_Device*, EI_CommandContext&, char const*, int)",
+                "TressFXHairObject::UpdateSimulationParameters(TressFXSimulationSettings const*, float)",
+                "TressFXHairObject::UpdateBoneMatrices(AMD::float4x4 const*, int)",
+                "TressFXSimulation::Simulate(EI_CommandContext&, std::vector<TressFXHairObject*, std::allocator<TressFXHairObject*> >&)",
+                "TressFXSDFCollision::Update(EI_CommandContext&, TressFXSDFCollisionSystem&)",
+                "TressFXSDFCollision::CollideWithHair(EI_CommandContext&, TressFXSDFCollisionSystem&, TressFXHairObject&)",
+                "TressFXAsset::LoadHairData(_IO_FILE*)", "TressFXAsset::GenerateFollowHairs(int, float, float)",
+                "TressFXAsset::ProcessAsset()", "TressFXAsset::LoadBoneData(_IO_FILE*, int, EI_Scene*)",
+                "TressFXBoneSkinning::LoadTressFXCollisionMeshData(EI_Scene*, char const*, int, char const*)"):
+        assert sym in out, sym

@@ -20,6 +20,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD_DIR = PKG / "_build"
 LIB_PATH = PKG / "libtfxgb300.so"
+HOST_DIR = PKG / "host"
+HOST_LIB_PATH = PKG / "libtressfx_host.so"   # the C++ host classes (include/tressfx/*.h)
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -99,7 +101,27 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         tmp = LIB_PATH.with_suffix(".so.tmp")
         _run([nvcc, "-shared", ARCH, "-o", str(tmp), *map(str, objects), "-lpthread", "-ldl", "-lrt"], verbose)
         os.replace(tmp, LIB_PATH)
+    build_host(verbose, force)
     return LIB_PATH
+
+
+def host_sources() -> list[Path]:
+    return sorted(HOST_DIR.glob("*.cpp"))
+
+
+def build_host(verbose: bool = False, force: bool = False) -> Path:
+    """Compile the C++ host classes into libtressfx_host.so, linked against libtfxgb300.so."""
+    srcs = host_sources()
+    deps = srcs + sorted(HOST_DIR.glob("*.h")) + sorted((ROOT / "include" / "tressfx").glob("*.h")) + \
+        [ROOT / "include" / "tressfx_gb300.h", LIB_PATH, Path(__file__)]
+    if not force and not _stale(HOST_LIB_PATH, deps):
+        return HOST_LIB_PATH
+    tmp = HOST_LIB_PATH.with_suffix(".so.tmp")
+    _run([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+          "-Wall", f"-I{ROOT / 'include'}", f"-I{HOST_DIR}", *map(str, srcs), "-o", str(tmp),
+          f"-L{PKG}", "-ltfxgb300", "-Wl,-rpath,$ORIGIN"], verbose)
+    os.replace(tmp, HOST_LIB_PATH)
+    return HOST_LIB_PATH
 
 
 if __name__ == "__main__":

@@ -22,11 +22,12 @@ struct BatchObject {
     const SdfFrame* sdfFrame;      // this frame's grid + margin (inside the device frame block)
 };
 
-// A group of up to 32 guide strands of one object: one block of the fused kernel at a time.
+// A group of guide strands of one object (at most fused_group_size(n)): one block of the fused
+// kernel at a time.
 struct WorkItem {
     int obj;         // index into the object table
     int firstGuide;  // first guide strand of the group
-    int count;       // guide strands in the group (<= 32)
+    int count;       // guide strands in the group
     int pad;
 };
 
@@ -56,6 +57,7 @@ struct FusedLaunch {
     const BatchObject* objs;
     const WorkItem* items;
     int numItems;
+    int* err;        // set to 1 when a block gives up waiting for its bulk copies
 };
 
 struct SdfBatchLaunch {
@@ -72,5 +74,6 @@ cudaError_t launch_batch_sdf(const SdfBatchLaunch& l, cudaStream_t s);
 bool fused_config_valid(int n, int vpl);
 int fused_smem_bytes(int n, int vpl, int warps);
 int fused_blocks_per_sm(int n, int vpl, int warps);
+int fused_group_size(int n);
 
 }  // namespace tfx

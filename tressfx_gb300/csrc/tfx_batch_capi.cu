@@ -67,6 +67,9 @@ struct tfx_batch_t {
     std::vector<BatchClass> classes;
     SdfBatchLaunch sdfL{};
 
+    int* devErr = nullptr;      // fused kernel: a block gave up waiting for its bulk copies
+    int* pinnedErr = nullptr;   // its copy at the end of each frame, one word per slot
+
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int launchesPerFrame = 0;
     std::string description;
@@ -93,6 +96,7 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
         if (b->pinned[i]) cudaFreeHost(b->pinned[i]);
         if (b->done[i]) cudaEventDestroy(b->done[i]);
     }
+    if (b->pinnedErr) cudaFreeHost(b->pinnedErr);
     if (b->devBlock) cudaFree(b->devBlock);
     if (b->devArena) cudaFree(b->devArena);
     for (auto& c : b->classes)
@@ -150,8 +154,8 @@ static void describe(tfx_batch b) {
     char buf[1024];
     int k = snprintf(buf, sizeof(buf), "sdf construct %d threads/block;", b->sdfL.constructThreads);
     for (auto& c : b->classes)
-        k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of 32;",
-                      c.n, c.vpl, c.warps, c.blocks, c.numItems);
+        k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d;",
+                      c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n));
     b->description = buf;
 }
 
@@ -160,7 +164,8 @@ static void make_items(tfx_batch b, BatchClass& c) {
     for (int o = 0; o < (int)b->hairs.size(); ++o) {
         tfx_hair h = b->hairs[o];
         if (h->n != c.n) continue;
-        for (int g = 0; g < h->G; g += 32) c.hostItems.push_back(WorkItem{o, g, std::min(32, h->G - g), 0});
+        const int gsz = fused_group_size(c.n);
+        for (int g = 0; g < h->G; g += gsz) c.hostItems.push_back(WorkItem{o, g, std::min(gsz, h->G - g), 0});
     }
     c.numItems = (int)c.hostItems.size();
 }
@@ -205,13 +210,19 @@ static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* 
     mark();
     for (auto& c : b->classes) {
         if (c.numItems == 0) continue;
-        FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems};
+        FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems, b->devErr};
         cudaError_t e = launch_fused_strands(fl, s);
         if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: fused strand launch");
         mark();
     }
     if (partMs) {
         cudaEventSynchronize(ev.back());
+        int flag = 0;
+        cudaMemcpy(&flag, b->devErr, sizeof(int), cudaMemcpyDeviceToHost);
+        if (flag) {
+            for (auto e : ev) cudaEventDestroy(e);
+            return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+        }
         partMs->clear();
         for (size_t i = 1; i < ev.size(); ++i) {
             float t = 0.f;
@@ -233,6 +244,10 @@ static int capture_graphs(tfx_batch b) {
         int r = TFX_OK;
         if (e != cudaSuccess) r = cuda_fail(e, "tfx_batch: capture upload");
         if (r == TFX_OK) r = launch_frame_direct(b, s, nullptr);
+        if (r == TFX_OK) {
+            e = cudaMemcpyAsync(b->pinnedErr + slot, b->devErr, sizeof(int), cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) r = cuda_fail(e, "tfx_batch: capture error-flag copy");
+        }
         cudaError_t ee = cudaStreamEndCapture(s, &g);
         if (r != TFX_OK) { if (g) cudaGraphDestroy(g); return r; }
         if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
@@ -391,11 +406,15 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         if (m) { ++b->nmeshes; b->totalMeshVerts += m->nverts; }
     const size_t sizes[3] = {sizeof(BatchObject) * nobj, sizeof(BatchMesh) * std::max(1, b->nmeshes),
                              sizeof(BatchSdf) * std::max(1, nsdf)};
-    TFX_CUDA(cudaMalloc(&b->devArena, align256(sizes[0]) + align256(sizes[1]) + align256(sizes[2])), "tfx_batch: tables");
+    TFX_CUDA(cudaMalloc(&b->devArena, align256(sizes[0]) + align256(sizes[1]) + align256(sizes[2]) + 256), "tfx_batch: tables");
     char* p = (char*)b->devArena;
     b->objTable = (BatchObject*)p; p += align256(sizes[0]);
     b->meshTable = (BatchMesh*)p; p += align256(sizes[1]);
-    b->sdfTable = (BatchSdf*)p;
+    b->sdfTable = (BatchSdf*)p; p += align256(sizes[2]);
+    b->devErr = (int*)p;
+    TFX_CUDA(cudaMemset(b->devErr, 0, sizeof(int)), "tfx_batch: clear error flag");
+    TFX_CUDA(cudaMallocHost((void**)&b->pinnedErr, 2 * sizeof(int)), "tfx_batch: pinned error flag");
+    b->pinnedErr[0] = b->pinnedErr[1] = 0;
 
     std::vector<BatchObject> objs(nobj);
     for (int o = 0; o < nobj; ++o) {
@@ -541,7 +560,10 @@ static int check_runnable(tfx_batch b, const char* who) {
 static int claim_block(tfx_batch b, int* slotOut) {
     const int s = b->slot;
     b->slot ^= 1;
-    if (b->used[s]) TFX_CUDA(cudaEventSynchronize(b->done[s]), "cudaEventSynchronize");
+    if (b->used[s]) {
+        TFX_CUDA(cudaEventSynchronize(b->done[s]), "cudaEventSynchronize");
+        if (b->pinnedErr[s]) return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+    }
     std::memcpy(b->pinned[s], b->staging.data(), b->blockBytes);
     *slotOut = s;
     return TFX_OK;

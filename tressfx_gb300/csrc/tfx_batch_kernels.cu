@@ -13,20 +13,24 @@
 //                           FloatFlip3 word.  The pairs and the encoding are the reference's, so the grid
 //                           is bit-identical.
 //  * k_fused_strands      - the six simulation stages (TressFXSimulation.hlsl:609-1001) and the SDF
-//                           collision (TressFXSDFCollision.hlsl:531-595) of a group of 32 guide
-//                           strands in one pass.  Phase 1 (all warps, L = n/VPL lanes per strand):
-//                           integration + global shape, strand-level data, VSP; positions and
-//                           bind-pose positions go to shared memory.  Phase 2 (warp 0, one lane per
-//                           strand): the local-shape sweeps, with the iterations software-pipelined
-//                           as a wavefront (iteration k runs two vertices behind iteration k-1, which
-//                           is exactly the order in which the sequential sweeps read and write).
-//                           Phase 3 (all warps): wind, length constraints (warp shuffles), tangents,
-//                           velocity clamp, follow hairs, collision, and the single write of every
-//                           buffer.  Blocks are persistent over the strand groups of every object of
-//                           one vertices-per-strand class.
+//                           collision (TressFXSDFCollision.hlsl:531-595) of a group of guide strands
+//                           (32, or 16 at n = 64) in one pass.  Phase 0: bulk asynchronous copies
+//                           (cp.async.bulk on an mbarrier) bring the group's Pos / Prev / InitialPos /
+//                           Tangent / RestLength rows into shared memory while warp 0 blends each
+//                           strand's bone matrix.  Phase 1a (one lane per strand): strand-level data.
+//                           Phase 1b (one thread per vertex): integration + global shape, VSP, bind
+//                           pose.  Phase 2 (one lane per strand, one warp per iteration): the
+//                           local-shape sweeps as a wavefront (iteration k runs two vertices behind
+//                           iteration k-1, which is exactly the order in which the sequential sweeps
+//                           read and write).  Phase 3a (n/VPL lanes per strand): wind, length
+//                           constraints (warp shuffles), tangents, velocity clamp.  Phase 3b (flat over
+//                           guide and follow vertices): follow hairs, collision, and the single write
+//                           of every buffer.  Blocks are persistent over the strand groups of every
+//                           object of one vertices-per-strand class.
 // All per-vertex arithmetic is the reference's, in the same order, so every buffer matches the
 // plain path and the oracle bit for bit.
 #include "tfx_batch.h"
+#include "tfx_bulk.cuh"
 #include "tfx_sdf_math.cuh"
 
 namespace tfx {
@@ -134,10 +138,51 @@ __global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __r
 // ============================================================================================
 // fused strand kernel
 //
-// Shared memory of one block (one group of 32 strands of n vertices; rows padded to 33 strands so
-// the sweep lanes and the vertex-parallel accesses are both conflict free):
-//   SP[n][33] float4  positions   SV[n][33] float4  Prev   BX/BY/BZ[n][33] float  bind-pose positions
-__host__ __device__ constexpr int fused_smem_for(int n) { return n * 33 * (16 + 16 + 12); }
+// One block runs one group of GS = fused_group_strands(N) guide strands of one object at a time.
+// Shared memory, strand-major rows of N vertices padded to N+1 float4, so that both the one-lane-per-
+// strand sweep and the one-lane-per-vertex passes are free of bank conflicts:
+//   TP[GS][N+1] positions   TV[GS][N+1] Prev   TI[GS][N+1] InitialPos, then bind pose   TT[GS][N+1] tangents
+//   TR[GS][N] rest lengths  SK[GS][4] blended bone matrix rows   SL[GS][3] StrandLevelData
+//   one mbarrier, on which the bulk copies that bring a group's rows in complete.
+__host__ __device__ constexpr int fused_group_strands(int n) { return n >= 64 ? 16 : 32; }
+__host__ __device__ constexpr int fused_smem_for(int n) {
+    return 4 * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * n * 4 + fused_group_strands(n) * 7 * 16 + 16;
+}
+constexpr int kFusedWaitPolls = 1 << 21;
+
+// IntegrationAndGlobalShapeConstraints (TressFXSimulation.hlsl:609-666) for vertex j: returns the new
+// position (after the global shape constraint) and, in `cur`, the position that becomes Prev.
+__device__ __forceinline__ float4 integrate_vertex(const DevSimConsts* __restrict__ c, const float (&m)[4][4], float4 ip,
+                                                   float4& cur, float4 old, int j, int n) {
+    float4 initialPos = ip;
+    const float3 sk = xform_row(xyz(initialPos), 1.0f, m);
+    initialPos.x = sk.x; initialPos.y = sk.y; initialPos.z = sk.z;
+    float4 currentPos = cur;
+    float4 shared = currentPos;
+    float4 oldPos = old;
+    if (c->reset != 0.0f) { currentPos = initialPos; oldPos = initialPos; }
+    if (currentPos.w > 0.0f) {
+        const float dt = c->timeStep;
+        const float gx = c->gravity * 0.0f, gy = c->gravity * -1.0f;
+        const float3 cu = xyz(currentPos), ol = xyz(oldPos);
+        const float3 force = mk3(gx, gy, gx);
+        const float3 r = add(add(cu, mul(c->decay, sub(cu, ol))), mul(mul(force, dt), dt));
+        shared.x = r.x; shared.y = r.y; shared.z = r.z;
+    } else {
+        shared = initialPos;
+    }
+    const float kG = c->globalStiffness, range = c->globalRange;
+    if (kG > 0.0f && range != 0.0f) {
+        if (shared.w > 0.0f) {
+            if ((float)j < range * (float)n) {
+                const float3 del = mul(kG, sub(xyz(initialPos), xyz(shared)));
+                shared.x = shared.x + del.x; shared.y = shared.y + del.y; shared.z = shared.z + del.z;
+            }
+        }
+    }
+    cur = currentPos;
+    return shared;
+}
 
 // One step of LocalShapeConstraints (TressFXSimulation.hlsl:794-825) for vertex j: pm1/pos are the
 // strand's vertices j-1 and j as this sweep has left them, pp1 vertex j+1 as the previous sweep left
@@ -159,31 +204,33 @@ __device__ __forceinline__ void bar_sync_first(int threads) {
     asm volatile("bar.sync 1, %0;" ::"r"(threads) : "memory");
 }
 
-// KW consecutive local-shape sweeps of the block's strands, as a wavefront over warps: warp k
+// KW consecutive local-shape sweeps of the group's strands, as a wavefront over warps: warp k
 // (k < KW) runs sweep k, lane s is strand s, and at time step t warp k works on vertex
 // j = t - 2k + 1.  Sweep k needs vertex j+1 as sweep k-1 left it, which warp k-1 stored at step t-1;
 // within one step no two warps touch the same element, and a barrier of the KW warps separates the
-// steps, so every read sees exactly the value the sequential sweeps give it.
-__device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const float* __restrict__ BX,
-                                                const float* __restrict__ BY, const float* __restrict__ BZ, int s,
-                                                bool active, int n, int k, int KW, float stiff) {
-    constexpr int LD = 33;
+// steps, so every read sees exactly the value the sequential sweeps give it.  Element (s, j) of a
+// tile is at s*RS + j.
+template <int N>
+__device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const float4* __restrict__ SB, int s, bool active,
+                                                int k, int KW, float stiff) {
+    constexpr int RS = N + 1;
+    float4* P = SP + s * RS;
+    const float4* B = SB + s * RS;
     float4 pm1 = make_float4(0.f, 0.f, 0.f, 0.f), pos = pm1;
     float3 bm1 = mk3(0.f, 0.f, 0.f), b0 = bm1;
-    const int T = (n - 2) + 2 * (KW - 1);
+    const int T = (N - 2) + 2 * (KW - 1);
     for (int t = 0; t < T; ++t) {
         const int j = t - 2 * k + 1;
-        if (active && j >= 1 && j <= n - 2) {
+        if (active && j >= 1 && j <= N - 2) {
             if (j == 1) {
-                pm1 = SP[s]; pos = SP[LD + s];
-                bm1 = mk3(BX[s], BY[s], BZ[s]);
-                b0 = mk3(BX[LD + s], BY[LD + s], BZ[LD + s]);
+                pm1 = P[0]; pos = P[1];
+                bm1 = xyz(B[0]); b0 = xyz(B[1]);
             }
-            float4 pp1 = SP[(j + 1) * LD + s];
-            const float3 bp1 = mk3(BX[(j + 1) * LD + s], BY[(j + 1) * LD + s], BZ[(j + 1) * LD + s]);
+            float4 pp1 = P[j + 1];
+            const float3 bp1 = xyz(B[j + 1]);
             local_shape_step(pm1, pos, pp1, bm1, b0, bp1, stiff);
-            SP[j * LD + s] = pos;
-            if (j == n - 2) SP[(n - 1) * LD + s] = pp1;
+            P[j] = pos;
+            if (j == N - 2) P[N - 1] = pp1;
             pm1 = pos; pos = pp1; bm1 = b0; b0 = bp1;
         }
         bar_sync_first(KW * 32);
@@ -191,100 +238,84 @@ __device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const f
 }
 
 template <int N, int VPL>
-__global__ void __launch_bounds__(256) k_fused_strands(const BatchObject* __restrict__ objs,
-                                                       const WorkItem* __restrict__ items, int numItems) {
-    constexpr int L = N / VPL;      // lanes per strand in the vertex phases
+__global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const BatchObject* __restrict__ objs,
+                                                                        const WorkItem* __restrict__ items, int numItems,
+                                                                        int* err) {
+    constexpr int GS = fused_group_strands(N);
+    constexpr int RS = N + 1;       // tile row stride, float4
+    constexpr int L = N / VPL;      // lanes per strand in the per-strand passes
     constexpr int SPW = 32 / L;     // strands per warp pass
-    constexpr int LD = 33;
     extern __shared__ float4 smem_f4[];
-    float4* SP = smem_f4;                                       // [N][LD]
-    float4* SV = SP + N * LD;                                   // [N][LD]
-    float* BX = reinterpret_cast<float*>(SV + N * LD);          // [N][LD] x3
-    float* BY = BX + N * LD;
-    float* BZ = BY + N * LD;
+    float4* TP = smem_f4;
+    float4* TV = TP + GS * RS;
+    float4* TI = TV + GS * RS;
+    float4* TT = TI + GS * RS;
+    float* TR = reinterpret_cast<float*>(TT + GS * RS);
+    float4* SK = reinterpret_cast<float4*>(TR + GS * N);
+    float4* SL = SK + GS * 4;
+    const uint32_t bar = smem_u32(SL + GS * 3);
 
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int lane = threadIdx.x & 31;
+    const int tid = threadIdx.x, nthreads = blockDim.x;
+    const int warp = tid >> 5, nwarps = nthreads >> 5;
+    const int lane = tid & 31;
     const int q = lane % L;         // lane within the strand
     const int slot = lane / L;      // strand slot within the warp pass
-    const int segBase = slot * L;   // first lane of this strand
 
-    for (int it = blockIdx.x; it < numItems; it += gridDim.x) {
+    if (tid == 0) mbar_init(bar, 1);
+    __syncthreads();
+
+    uint32_t parity = 0;
+    for (int it = blockIdx.x; it < numItems; it += gridDim.x, parity ^= 1u) {
         const WorkItem wi = items[it];
         const BatchObject& ob = objs[wi.obj];
-        const HairView& h = ob.hair;
+        const HairView h = ob.hair;
         const DevSimConsts* __restrict__ c = ob.consts;
         const int F = h.F;
-        const float dt = c->timeStep;
+        const int count = wi.count;
+        const int gs0 = wi.firstGuide * (F + 1);   // strand index of the group's first guide
 
-        // ============================================================ phase 1
-        for (int pass = warp; pass * SPW < wi.count; pass += nwarps) {
-            const int s = pass * SPW + slot;   // strand within the group
-            const bool active = s < wi.count;
-            const int g = wi.firstGuide + s;
-            const int gs = g * (F + 1);
-            const int base = gs * N + q * VPL;
-            float4 p[VPL], pv[VPL], ppv[VPL], ip[VPL];
+        // ------------------------------------------------------------ phase 0: bring the group in
+        float4 bq4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (warp == 0) {
+            if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)count * (uint32_t)(4 * N * 16 + N * 4));
+            __syncwarp();
+            if (lane < count) {
+                const size_t vo = (size_t)(gs0 + lane * (F + 1)) * N;
+                bulk_g2s(smem_u32(TP + lane * RS), h.pos + vo, N * 16, bar);
+                bulk_g2s(smem_u32(TV + lane * RS), h.prev + vo, N * 16, bar);
+                bulk_g2s(smem_u32(TI + lane * RS), h.init + vo, N * 16, bar);
+                bulk_g2s(smem_u32(TT + lane * RS), h.tan + vo, N * 16, bar);
+                bulk_g2s(smem_u32(TR + lane * N), h.rest + vo, N * 4, bar);
+                // strand level, while the rows are in flight: the blended bone matrix and its quaternion
+                const int gs = gs0 + lane * (F + 1);
+                float m[4][4];
+                blend_bones(c->bones, __ldg(h.skin + 2 * gs), __ldg(h.skin + 2 * gs + 1), m);
 #pragma unroll
-            for (int k = 0; k < VPL; ++k) {
-                if (active) {
-                    p[k] = h.pos[base + k];
-                    ppv[k] = h.prev[base + k];
-                    ip[k] = __ldg(h.init + base + k);
-                } else {
-                    p[k] = ppv[k] = ip[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                }
+                for (int r = 0; r < 4; ++r) SK[lane * 4 + r] = make_float4(m[r][0], m[r][1], m[r][2], m[r][3]);
+                const Q4 bq = quat_from_matrix(m);
+                bq4 = make_float4(bq.x, bq.y, bq.z, bq.w);
             }
-            const float4 sidx = active ? __ldg(h.skin + 2 * gs) : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 swt = active ? __ldg(h.skin + 2 * gs + 1) : make_float4(1.f, 0.f, 0.f, 0.f);
+        }
+        const bool arrived = mbar_wait_bounded(bar, parity, kFusedWaitPolls);
+        if (__syncthreads_or(!arrived)) {
+            if (tid == 0) atomicOr(err, 1);
+            mbar_wait_bounded(bar, parity, kFusedWaitPolls);   // let copies still in flight land
+            return;
+        }
+
+        // ------------------------------------------------------------ phase 1a: CalculateStrandLevelData
+        if (warp == 0 && lane < count) {
+            const int s = lane, gs = gs0 + s * (F + 1);
             float m[4][4];
-            blend_bones(c->bones, sidx, swt, m);
-
-            // IntegrationAndGlobalShapeConstraints
-            const bool reset = c->reset != 0.0f;
-            const float kG = c->globalStiffness, range = c->globalRange;
 #pragma unroll
-            for (int k = 0; k < VPL; ++k) {
-                const int j = q * VPL + k;
-                float4 initialPos = ip[k];
-                const float3 sk = xform_row(xyz(initialPos), 1.0f, m);
-                initialPos.x = sk.x; initialPos.y = sk.y; initialPos.z = sk.z;
-                float4 currentPos = p[k];
-                float4 shared = currentPos;
-                float4 oldPos = ppv[k];
-                if (reset) { currentPos = initialPos; oldPos = initialPos; }
-                if (currentPos.w > 0.0f) {
-                    const float gx = c->gravity * 0.0f, gy = c->gravity * -1.0f;
-                    const float3 cur = xyz(currentPos), old = xyz(oldPos);
-                    const float3 force = mk3(gx, gy, gx);
-                    const float3 r = add(add(cur, mul(c->decay, sub(cur, old))), mul(mul(force, dt), dt));
-                    shared.x = r.x; shared.y = r.y; shared.z = r.z;
-                } else {
-                    shared = initialPos;
-                }
-                if (kG > 0.0f && range != 0.0f) {
-                    if (shared.w > 0.0f) {
-                        if ((float)j < range * (float)N) {
-                            const float3 del = mul(kG, sub(xyz(initialPos), xyz(shared)));
-                            shared.x = shared.x + del.x; shared.y = shared.y + del.y; shared.z = shared.z + del.z;
-                        }
-                    }
-                }
-                pv[k] = currentPos;
-                p[k] = shared;
-                if (active) h.prevprev[base + k] = ppv[k];
+            for (int r = 0; r < 4; ++r) {
+                const float4 row = SK[s * 4 + r];
+                m[r][0] = row.x; m[r][1] = row.y; m[r][2] = row.z; m[r][3] = row.w;
             }
-
-            // CalculateStrandLevelData: vertices 0 and 1 after integration
-            float4 oo1, o0, o1, n0, n1;
-            if constexpr (VPL == 1) {
-                const int l1 = segBase + 1;
-                oo1 = shfl4(ppv[0], l1); o1 = shfl4(pv[0], l1); n1 = shfl4(p[0], l1);
-                o0 = shfl4(pv[0], segBase); n0 = shfl4(p[0], segBase);
-            } else {
-                oo1 = shfl4(ppv[1], segBase); o1 = shfl4(pv[1], segBase); n1 = shfl4(p[1], segBase);
-                o0 = shfl4(pv[0], segBase); n0 = shfl4(p[0], segBase);
-            }
+            float4 o0 = TP[s * RS], o1 = TP[s * RS + 1];
+            const float4 oo1 = TV[s * RS + 1];
+            const float4 n0 = integrate_vertex(c, m, TI[s * RS], o0, TV[s * RS], 0, N);
+            const float4 n1 = integrate_vertex(c, m, TI[s * RS + 1], o1, oo1, 1, N);
             const float3 u = normalize(sub(xyz(o1), xyz(o0)));
             const float3 v = normalize(sub(xyz(n1), xyz(n0)));
             const Q4 rot = qfrom2(u, v);
@@ -298,71 +329,73 @@ __global__ void __launch_bounds__(256) k_fused_strands(const BatchObject* __rest
                 const float accel = sqrtf(ax * ax + ay * ay + az * az + aw * aw);
                 if (accel > c->vspAccelThreshold) vspCoeff = 1.0f;
             }
-            const Q4 bq = quat_from_matrix(m);
-            if (active && q == 0) {
-                h.sld[3 * gs + 0] = make_float4(bq.x, bq.y, bq.z, bq.w);
-                h.sld[3 * gs + 1] = make_float4(rot.x, rot.y, rot.z, rot.w);
-                h.sld[3 * gs + 2] = make_float4(trans.x, trans.y, trans.z, vspCoeff);
-            }
-
-            // VelocityShockPropagation, then hand over to shared memory
-#pragma unroll
-            for (int k = 0; k < VPL; ++k) {
-                const int j = q * VPL + k;
-                if (j >= 2) {
-                    const float3 a = add(mul(1.0f - vspCoeff, xyz(p[k])), mul(vspCoeff, add(qrot(rot, xyz(p[k])), trans)));
-                    const float3 b = add(mul(1.0f - vspCoeff, xyz(pv[k])), mul(vspCoeff, add(qrot(rot, xyz(pv[k])), trans)));
-                    p[k] = with_xyz(p[k], a);
-                    pv[k] = with_xyz(pv[k], b);
-                }
-                if (active) {
-                    SP[j * LD + s] = p[k];
-                    SV[j * LD + s] = pv[k];
-                    const float3 bp = qrot(bq, xyz(ip[k]));
-                    BX[j * LD + s] = bp.x; BY[j * LD + s] = bp.y; BZ[j * LD + s] = bp.z;
-                }
-            }
+            const float4 r4 = make_float4(rot.x, rot.y, rot.z, rot.w);
+            const float4 t4 = make_float4(trans.x, trans.y, trans.z, vspCoeff);
+            SL[s * 3 + 0] = bq4; SL[s * 3 + 1] = r4; SL[s * 3 + 2] = t4;
+            h.sld[3 * gs + 0] = bq4; h.sld[3 * gs + 1] = r4; h.sld[3 * gs + 2] = t4;
         }
         __syncthreads();
 
-        // ============================================================ phase 2: LocalShapeConstraints
+        // ------------------------------------------------------------ phase 1b: integration, VSP, bind pose
+        for (int e = tid; e < count * N; e += nthreads) {
+            const int s = e / N, j = e % N;
+            const int x = s * RS + j;
+            float m[4][4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float4 row = SK[s * 4 + r];
+                m[r][0] = row.x; m[r][1] = row.y; m[r][2] = row.z; m[r][3] = row.w;
+            }
+            const float4 ip = TI[x], old = TV[x];
+            float4 pv = TP[x];
+            float4 p = integrate_vertex(c, m, ip, pv, old, j, N);
+            h.prevprev[(size_t)(gs0 + s * (F + 1)) * N + j] = old;
+            if (j >= 2) {
+                const float4 r4 = SL[s * 3 + 1], t4 = SL[s * 3 + 2];
+                const Q4 rot{r4.x, r4.y, r4.z, r4.w};
+                const float3 trans = xyz(t4);
+                const float vspCoeff = t4.w;
+                const float3 a = add(mul(1.0f - vspCoeff, xyz(p)), mul(vspCoeff, add(qrot(rot, xyz(p)), trans)));
+                const float3 b = add(mul(1.0f - vspCoeff, xyz(pv)), mul(vspCoeff, add(qrot(rot, xyz(pv)), trans)));
+                p = with_xyz(p, a);
+                pv = with_xyz(pv, b);
+            }
+            TP[x] = p;
+            TV[x] = pv;
+            const float4 b4 = SL[s * 3 + 0];
+            const float3 bp = qrot(Q4{b4.x, b4.y, b4.z, b4.w}, xyz(ip));
+            TI[x] = make_float4(bp.x, bp.y, bp.z, 0.0f);
+        }
+        __syncthreads();
+
+        // ------------------------------------------------------------ phase 2: LocalShapeConstraints
         const int lsIters = c->reserved0;
         if (lsIters > 0) {
             const float stiff = 0.5f * fminf(c->localStiffness, 0.95f);
             for (int done = 0; done < lsIters;) {   // waves of up to one sweep per warp
                 const int KW = min(lsIters - done, nwarps);
-                if (warp < KW) sweep_wavefront(SP, BX, BY, BZ, lane, lane < wi.count, N, warp, KW, stiff);
+                if (warp < KW) sweep_wavefront<N>(TP, TI, lane, lane < count, warp, KW, stiff);
                 __syncthreads();
                 done += KW;
             }
-        } else {
-            __syncthreads();
         }
 
-        // ============================================================ phase 3
-        const float* sdf = ob.sdf;
-        SdfGrid sg;
-        float margin = 0.0f;
-        if (sdf) {
-            sg = ob.sdfFrame->grid;
-            margin = ob.sdfFrame->margin;
-        }
-        for (int pass = warp; pass * SPW < wi.count; pass += nwarps) {
+        // ------------------------------------------------------------ phase 3a: wind, length, tangents, clamp
+        const float dt = c->timeStep;
+        for (int pass = warp; pass * SPW < count; pass += nwarps) {
             const int s = pass * SPW + slot;
-            const bool active = s < wi.count;
-            const int g = wi.firstGuide + s;
-            const int gs = g * (F + 1);
-            const int base = gs * N + q * VPL;
+            const bool active = s < count;
+            const int gs = gs0 + s * (F + 1);
+            const int base = s * RS + q * VPL;
             float4 p[VPL], pv[VPL], tn[VPL];
             float len[VPL];
 #pragma unroll
             for (int k = 0; k < VPL; ++k) {
-                const int j = q * VPL + k;
                 if (active) {
-                    p[k] = SP[j * LD + s];
-                    pv[k] = SV[j * LD + s];
-                    tn[k] = h.tan[base + k];
-                    len[k] = __ldg(h.rest + base + k);
+                    p[k] = TP[base + k];
+                    pv[k] = TV[base + k];
+                    tn[k] = TT[base + k];
+                    len[k] = TR[s * N + q * VPL + k];
                 } else {
                     p[k] = pv[k] = tn[k] = make_float4(0.f, 0.f, 0.f, 0.f);
                     len[k] = 0.0f;
@@ -466,44 +499,84 @@ __global__ void __launch_bounds__(256) k_fused_strands(const BatchObject* __rest
                 }
             }
             if (active) {
-                // UpdateFollowHairVertices from the constrained guide, each follow collided at once
-                const float tip = c->tipSeparation;
-                for (int i = 0; i < F; ++i) {
-                    const int fs = gs + i + 1;
-                    const float4 off = __ldg(h.followOffset + fs);
-#pragma unroll
-                    for (int k = 0; k < VPL; ++k) {
-                        const int j = q * VPL + k;
-                        const int fv = fs * N + j;
-                        const float factor = tip * ((float)j / (float)N) + 1.0f;
-                        float3 fp = add(xyz(p[k]), mul(factor, xyz(off)));
-                        const float4 oldF = h.pos[fv];
-                        h.tan[fv] = tn[k];
-                        float3 proj;
-                        if (sdf && j >= 2 && sdf_collide_point(sdf, sg, margin, fp, proj)) {
-                            fp = proj;
-                            const float4 pf = h.prev[fv];
-                            h.prev[fv] = with_xyz(pf, proj);
-                        }
-                        h.pos[fv] = with_xyz(oldF, fp);
-                    }
-                }
-                // guide collision and the final writes
 #pragma unroll
                 for (int k = 0; k < VPL; ++k) {
-                    const int j = q * VPL + k;
-                    float3 proj;
-                    if (sdf && j >= 2 && sdf_collide_point(sdf, sg, margin, xyz(p[k]), proj)) {
-                        p[k] = with_xyz(p[k], proj);
-                        pv[k] = with_xyz(pv[k], proj);
-                    }
-                    h.pos[base + k] = p[k];
-                    h.prev[base + k] = pv[k];
-                    h.tan[base + k] = tn[k];
+                    TP[base + k] = p[k];
+                    TV[base + k] = pv[k];
+                    TT[base + k] = tn[k];
                 }
             }
         }
-        __syncthreads();   // shared memory is reused by the next group
+        __syncthreads();
+
+        // ------------------------------------------------------------ phase 3b: follow hairs, collision, writes
+        // Flat over the group's (strand, hair, vertex) elements; element e of guide s is global vertex
+        // (gs0 + s*(F+1))*N + e%((F+1)*N): hair 0 is the guide, hairs 1..F its follows
+        // (UpdateFollowHairVertices, TressFXSimulation.hlsl:978-1001), every vertex then collided
+        // (CollideHairVerticesWithSdf_forward, TressFXSDFCollision.hlsl:531-595).  Four elements per
+        // thread are loaded before any is written, so their loads overlap.
+        {
+            const float* __restrict__ sdf = ob.sdf;
+            SdfGrid sg = SdfGrid{0.f, 0.f, 0.f, 1.f, 0, 0, 0, 0};
+            float margin = 0.0f;
+            if (sdf) { sg = ob.sdfFrame->grid; margin = ob.sdfFrame->margin; }
+            const float tip = c->tipSeparation;
+            const int rowLen = (F + 1) * N;
+            const int E = count * rowLen;
+            constexpr int U = 4;
+            for (int e0 = tid; e0 < E; e0 += U * nthreads) {
+                float3 pt[U];
+                float wU[U], dist[U];
+                int vg[U], xs[U], jj[U], hh[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int e = e0 + u * nthreads;
+                    hh[u] = -1;
+                    if (e < E) {
+                        const int s = e / rowLen, r = e - s * rowLen;
+                        const int i = r / N, j = r % N;
+                        const int gs = gs0 + s * (F + 1);
+                        const int x = s * RS + j;
+                        hh[u] = i; jj[u] = j; xs[u] = x;
+                        vg[u] = gs * N + r;
+                        const float4 gp = TP[x];
+                        if (i == 0) {
+                            pt[u] = xyz(gp);
+                            wU[u] = gp.w;
+                        } else {
+                            const float4 off = __ldg(h.followOffset + gs + i);
+                            const float factor = tip * ((float)j / (float)N) + 1.0f;
+                            pt[u] = add(xyz(gp), mul(factor, xyz(off)));
+                            // inverse mass of the follow vertex: no thread writes this word before this read
+                            wU[u] = __ldg(&h.pos[vg[u]].w);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    dist[u] = 1e10f;
+                    if (hh[u] >= 0 && sdf && jj[u] >= 2) dist[u] = sdf_lookup(sdf, sg, pt[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (hh[u] < 0) continue;
+                    float3 proj = pt[u];
+                    const bool hit = sdf && jj[u] >= 2 && sdf_collide_from(sdf, sg, margin, pt[u], dist[u], proj);
+                    const float3 fin = hit ? proj : pt[u];
+                    const int v = vg[u];
+                    h.pos[v] = make_float4(fin.x, fin.y, fin.z, wU[u]);
+                    h.tan[v] = TT[xs[u]];
+                    if (hh[u] == 0) {
+                        const float4 pv = TV[xs[u]];
+                        h.prev[v] = hit ? with_xyz(pv, proj) : pv;
+                    } else if (hit) {
+                        h.prev[v] = with_xyz(h.prev[v], proj);
+                    }
+                }
+            }
+        }
+        fence_proxy_async_smem();   // this group's shared-memory accesses come before the next group's copies
+        __syncthreads();
     }
 }
 
@@ -512,7 +585,8 @@ __global__ void __launch_bounds__(256) k_fused_strands(const BatchObject* __rest
 template <int N, int VPL>
 static cudaError_t launch_fused_nv(const FusedLaunch& fl, cudaStream_t s) {
     // the dynamic shared-memory attribute is set by fused_blocks_per_sm before the first launch
-    k_fused_strands<N, VPL><<<fl.blocks, fl.warpsPerBlock * 32, fused_smem_for(N), s>>>(fl.objs, fl.items, fl.numItems);
+    k_fused_strands<N, VPL><<<fl.blocks, fl.warpsPerBlock * 32, fused_smem_for(N), s>>>(fl.objs, fl.items, fl.numItems,
+                                                                                        fl.err);
     return cudaGetLastError();
 }
 
@@ -525,6 +599,7 @@ bool fused_config_valid(int n, int vpl) {
 }
 
 int fused_smem_bytes(int n, int, int) { return fused_smem_for(n); }
+int fused_group_size(int n) { return fused_group_strands(n); }
 
 #define TFX_FUSED_CASE(NN, VV) \
     if (fl.n == NN && fl.vpl == VV) return launch_fused_nv<NN, VV>(fl, s);
@@ -551,6 +626,8 @@ cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s) {
         int nb = 0;                                                                                               \
         cudaError_t e = cudaFuncSetAttribute(k_fused_strands<NN, VV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                              fused_smem_for(NN));                                                 \
+        if (e != cudaSuccess) return 0;                                                                           \
+        e = cudaFuncSetAttribute(k_fused_strands<NN, VV>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);    \
         if (e != cudaSuccess) return 0;                                                                           \
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused_strands<NN, VV>, warps * 32, fused_smem_for(NN)); \
         return nb;                                                                                                \

@@ -166,6 +166,23 @@ __device__ __forceinline__ float sdf_lookup(const float* __restrict__ sdf, const
 
 // CollideHairVerticesWithSdf_forward for one vertex (j >= 2): returns true and the projected
 // position when the vertex is pushed out (then Pos.xyz and Prev.xyz both take it).
+// The part after the first lookup: `distance` = sdf_lookup(sdf, g, p).
+__device__ __forceinline__ bool sdf_collide_from(const float* __restrict__ sdf, const SdfGrid& g, float margin, float3 p,
+                                                 float distance, float3& proj) {
+    if (distance > margin) return false;
+    const float h = 0.1f * g.cell;
+    const float fx = sdf_lookup(sdf, g, add(p, mul(mk3(1.0f, 0.0f, 0.0f), h)));
+    const float fy = sdf_lookup(sdf, g, add(p, mul(mk3(0.0f, 1.0f, 0.0f), h)));
+    const float fz = sdf_lookup(sdf, g, add(p, mul(mk3(0.0f, 0.0f, 1.0f), h)));
+    const float3 grad = mk3((fx - distance) / h, (fy - distance) / h, (fz - distance) / h);
+    const float3 nrm = normalize(grad);
+    if (distance < margin) {
+        proj = add(p, mul(nrm, margin - distance));
+        return true;
+    }
+    return false;
+}
+
 __device__ __forceinline__ bool sdf_collide_point(const float* __restrict__ sdf, const SdfGrid& g, float margin, float3 p,
                                                   float3& proj) {
     const float distance = sdf_lookup(sdf, g, p);
