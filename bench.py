@@ -144,16 +144,29 @@ def plain_kernel_bytes(scene) -> dict[str, float]:
     return out
 
 
-def fused_bytes(scene) -> dict[int, float]:
-    """Algorithmic HBM bytes per frame of the fused strand kernel of each n class: read Pos, Prev,
-    InitialPos, RestLength and write Pos, Prev, PrevPrev, Tangent of every guide vertex (116 B);
-    write Pos and Tangent of every follow vertex (32 B); per guide strand the skinning record, the
-    strand-level record and the follow root offsets."""
+def strand_bytes(scene) -> dict[int, float]:
+    """Algorithmic HBM bytes per frame of k_fused_strands for each n class: read Pos, Prev,
+    InitialPos, Tangent (its w is kept) and RestLength, write Pos, Prev, PrevPrev and Tangent of
+    every guide vertex (132 B); per guide strand the skinning record and the strand-level record
+    (80 B)."""
+    out: dict[int, float] = {}
+    for o in scene.objects:
+        a = o.asset
+        G, n = a.num_guide_strands, a.verts_per_strand
+        out[n] = out.get(n, 0.0) + 132 * G * n + 80 * G
+    return out
+
+
+def follow_bytes(scene) -> dict[int, float]:
+    """Algorithmic HBM bytes per frame of k_follow_collide for each n class: read the guide's Pos
+    and Tangent (32 B per guide vertex); per follow vertex read its inverse mass (4 B) and write Pos
+    and Tangent (32 B); per follow strand its root offset (16 B); every SDF cell once (4 B)."""
     out: dict[int, float] = {}
     for o in scene.objects:
         a = o.asset
         G, n, F = a.num_guide_strands, a.verts_per_strand, a.follow_per_guide
-        out[n] = out.get(n, 0.0) + 116 * G * n + 32 * F * G * n + G * (32 + 48 + 16 * F)
+        cells = int(np.prod(o.sdf_dims)) if o.mesh is not None else 0
+        out[n] = out.get(n, 0.0) + 32 * G * n + 36 * F * G * n + 16 * F * G + 4 * cells
     return out
 
 
@@ -386,28 +399,36 @@ def main() -> None:
         cpu = {"value": scene.vertices_per_frame * fr / el, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
                "sample": f"{fr} full frames of the workload after one untimed frame ({el:.1f} s, oracle restatement)"}
         peaks = load_peaks()
-        fb = fused_bytes(scene)
-        classes = sorted(fb)
+        sb, fbw = strand_bytes(scene), follow_bytes(scene)
+        classes = sorted(sb)
         part = b["part_ms"]
+        nc = len(classes)
         kern = {"mesh_skin+sdf_build": part[0]}
-        for n, ms_k in zip(classes, part[1:]):
-            kern[f"fused_strands_n{n}"] = ms_k
-        dom_n = max(classes, key=lambda n: part[1 + classes.index(n)])
-        dom_ms = part[1 + classes.index(dom_n)]
-        achieved = fb[dom_n] / (dom_ms * 1e-3) / 1e9
+        gbs = {}
+        for i, n in enumerate(classes):
+            kern[f"fused_strands_n{n}"] = part[1 + i]
+            kern[f"follow_collide_n{n}"] = part[1 + nc + i]
+            gbs[f"fused_strands_n{n}"] = sb[n] / (part[1 + i] * 1e-3) / 1e9
+            gbs[f"follow_collide_n{n}"] = fbw[n] / (part[1 + nc + i] * 1e-3) / 1e9
+        hbm_parts = [(f"k_fused_strands (n={n})", part[1 + i], sb[n]) for i, n in enumerate(classes)] + \
+                    [(f"k_follow_collide (n={n})", part[1 + nc + i], fbw[n]) for i, n in enumerate(classes)]
+        dom_name, dom_ms, dom_bytes = max(hbm_parts, key=lambda t: t[1])
+        achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
         line = {
             "metric": metric, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": dict(base_cfg, path="batched: one CUDA graph per frame (mesh skinning, tiled SDF build, "
-                                          "fused persistent strand kernel per n class)", shapes=b["describe"]),
+            "config": dict(base_cfg, path="batched: one CUDA graph per frame (mesh skinning + SDF build on one "
+                                          "branch, concurrent with the fused strand kernel per n class; then follow "
+                                          "hairs + collision)", shapes=b["describe"]),
             "e2e": {"value": b["e2e_value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": b["h2d"],
                     "d2h_bytes_per_step": b["d2h"], "ms_per_step": b["e2e_ms_per_step"]},
             "gpu_launches": b["launches_per_frame"] * args.steps,
-            "roofline": {"bound": "hbm", "kernel": f"k_fused_strands (n={dom_n})", "achieved": achieved,
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved,
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                         "peak_source": peaks["source"], "algorithmic_bytes": fb[dom_n], "launch_ms": dom_ms},
+                         "peak_source": peaks["source"], "algorithmic_bytes": dom_bytes, "launch_ms": dom_ms},
             "kernel_ms": kern,
+            "kernel_gbs": gbs,
             "cpu_baseline": cpu,
             "clocks": dict(b["clocks"], window="the timed frames repeated for 1.2 s"),
         }

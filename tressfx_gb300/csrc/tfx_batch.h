@@ -60,6 +60,13 @@ struct FusedLaunch {
     int* err;        // set to 1 when a block gives up waiting for its bulk copies
 };
 
+struct FollowLaunch {
+    int n, blocks;
+    const BatchObject* objs;
+    const WorkItem* items;
+    int numItems;
+};
+
 struct SdfBatchLaunch {
     const BatchSdf* sdfs;
     int nsdf;
@@ -69,11 +76,13 @@ struct SdfBatchLaunch {
 };
 
 cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s);
+cudaError_t launch_follow_collide(const FollowLaunch& fl, cudaStream_t s);
 cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s);
 cudaError_t launch_batch_sdf(const SdfBatchLaunch& l, cudaStream_t s);
 bool fused_config_valid(int n, int vpl);
 int fused_smem_bytes(int n, int vpl, int warps);
 int fused_blocks_per_sm(int n, int vpl, int warps);
 int fused_group_size(int n);
+int follow_blocks_per_sm(int n);
 
 }  // namespace tfx

@@ -31,6 +31,8 @@ using namespace tfx;
 struct BatchClass {
     int n = 0;
     int vpl = 1, warps = 8, blocks = 1;
+    int perSMCap = 0;            // resident strand blocks per SM allowed (0 = as many as fit)
+    int followBlocks = 1;        // grid of k_follow_collide
     std::vector<WorkItem> hostItems;
     WorkItem* items = nullptr;  // device
     int numItems = 0;
@@ -67,6 +69,8 @@ struct tfx_batch_t {
     std::vector<BatchClass> classes;
     SdfBatchLaunch sdfL{};
 
+    cudaStream_t side = nullptr;             // second capture branch: mesh skinning + SDF build
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     int* devErr = nullptr;      // fused kernel: a block gave up waiting for its bulk copies
     int* pinnedErr = nullptr;   // its copy at the end of each frame, one word per slot
 
@@ -97,6 +101,9 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
         if (b->done[i]) cudaEventDestroy(b->done[i]);
     }
     if (b->pinnedErr) cudaFreeHost(b->pinnedErr);
+    if (b->evFork) cudaEventDestroy(b->evFork);
+    if (b->evJoin) cudaEventDestroy(b->evJoin);
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->devBlock) cudaFree(b->devBlock);
     if (b->devArena) cudaFree(b->devArena);
     for (auto& c : b->classes)
@@ -156,6 +163,8 @@ static void describe(tfx_batch b) {
     for (auto& c : b->classes)
         k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d;",
                       c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n));
+    k += snprintf(buf + k, sizeof(buf) - k, " SDF build %s the strand kernels;",
+                  b->side ? "concurrent with" : "before");
     b->description = buf;
 }
 
@@ -181,15 +190,44 @@ static int upload_items(BatchClass& c) {
 
 // Grid of a fused class: as many resident blocks as fit (persistent), no more than groups.
 static int size_class(tfx_batch b, BatchClass& c) {
-    const int perSM = fused_blocks_per_sm(c.n, c.vpl, c.warps);
+    int perSM = fused_blocks_per_sm(c.n, c.vpl, c.warps);
     if (perSM <= 0)
         return fail(TFX_ERR_CUDA, "tfx_batch: fused kernel n=%d vpl=%d with %d warps cannot be resident", c.n, c.vpl, c.warps);
+    if (c.perSMCap > 0) perSM = std::min(perSM, c.perSMCap);
     c.blocks = std::max(1, std::min(perSM * b->ctx->numSMs, c.numItems));
+    const int fpSM = std::max(1, follow_blocks_per_sm(c.n));
+    c.followBlocks = std::max(1, std::min(fpSM * b->ctx->numSMs, c.numItems));
     return TFX_OK;
 }
 
+static int launch_sdf_part(tfx_batch b, cudaStream_t s) {
+    if (b->totalMeshVerts > 0) {
+        cudaError_t e = launch_batch_mesh_skin(b->meshTable, b->nmeshes, b->totalMeshVerts, s);
+        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: mesh skinning launch");
+    }
+    if (!b->sdfs.empty()) {
+        cudaError_t e = launch_batch_sdf(b->sdfL, s);
+        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: SDF launch");
+    }
+    return TFX_OK;
+}
+
+static int launch_strands(tfx_batch b, BatchClass& c, cudaStream_t s) {
+    FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems, b->devErr};
+    cudaError_t e = launch_fused_strands(fl, s);
+    return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: fused strand launch");
+}
+
+static int launch_follows(tfx_batch b, BatchClass& c, cudaStream_t s) {
+    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems};
+    cudaError_t e = launch_follow_collide(fl, s);
+    return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: follow/collide launch");
+}
+
+// One frame as direct launches, in dependency order on one stream, with an event after each part:
+// part 0 = mesh skinning + SDF build, then one part per class for k_fused_strands, then one per
+// class for k_follow_collide (used by profiling).
 static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* partMs) {
-    // the body of a frame without the block upload (used by capture, profiling and autotuning)
     std::vector<cudaEvent_t> ev;
     auto mark = [&]() {
         if (!partMs) return;
@@ -199,20 +237,16 @@ static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* 
         ev.push_back(e);
     };
     mark();
-    if (b->totalMeshVerts > 0) {
-        cudaError_t e = launch_batch_mesh_skin(b->meshTable, b->nmeshes, b->totalMeshVerts, s);
-        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: mesh skinning launch");
-    }
-    if (!b->sdfs.empty()) {
-        cudaError_t e = launch_batch_sdf(b->sdfL, s);
-        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: SDF launch");
-    }
+    if (int r = launch_sdf_part(b, s)) return r;
     mark();
     for (auto& c : b->classes) {
         if (c.numItems == 0) continue;
-        FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems, b->devErr};
-        cudaError_t e = launch_fused_strands(fl, s);
-        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: fused strand launch");
+        if (int r = launch_strands(b, c, s)) return r;
+        mark();
+    }
+    for (auto& c : b->classes) {
+        if (c.numItems == 0) continue;
+        if (int r = launch_follows(b, c, s)) return r;
         mark();
     }
     if (partMs) {
@@ -234,6 +268,28 @@ static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* 
     return TFX_OK;
 }
 
+// The frame body as captured into the graph: the SDF branch (mesh skinning + SDF build) on the side
+// stream runs concurrently with the strand kernels, which need no SDF; k_follow_collide waits for both.
+static int launch_frame_forked(tfx_batch b, cudaStream_t s) {
+    const bool fork = b->side && !b->sdfs.empty();
+    if (fork) {
+        TFX_CUDA(cudaEventRecord(b->evFork, s), "tfx_batch: fork");
+        TFX_CUDA(cudaStreamWaitEvent(b->side, b->evFork, 0), "tfx_batch: fork");
+        if (int r = launch_sdf_part(b, b->side)) return r;
+        TFX_CUDA(cudaEventRecord(b->evJoin, b->side), "tfx_batch: join");
+    } else if (int r = launch_sdf_part(b, s)) {
+        return r;
+    }
+    for (auto& c : b->classes)
+        if (c.numItems > 0)
+            if (int r = launch_strands(b, c, s)) return r;
+    if (fork) TFX_CUDA(cudaStreamWaitEvent(s, b->evJoin, 0), "tfx_batch: join");
+    for (auto& c : b->classes)
+        if (c.numItems > 0)
+            if (int r = launch_follows(b, c, s)) return r;
+    return TFX_OK;
+}
+
 static int capture_graphs(tfx_batch b) {
     cudaStream_t s = b->ctx->stream;
     for (int slot = 0; slot < 2; ++slot) {
@@ -243,7 +299,7 @@ static int capture_graphs(tfx_batch b) {
         cudaError_t e = cudaMemcpyAsync(b->devBlock, b->pinned[slot], b->blockBytes, cudaMemcpyHostToDevice, s);
         int r = TFX_OK;
         if (e != cudaSuccess) r = cuda_fail(e, "tfx_batch: capture upload");
-        if (r == TFX_OK) r = launch_frame_direct(b, s, nullptr);
+        if (r == TFX_OK) r = launch_frame_forked(b, s);
         if (r == TFX_OK) {
             e = cudaMemcpyAsync(b->pinnedErr + slot, b->devErr, sizeof(int), cudaMemcpyDeviceToHost, s);
             if (e != cudaSuccess) r = cuda_fail(e, "tfx_batch: capture error-flag copy");
@@ -256,7 +312,7 @@ static int capture_graphs(tfx_batch b) {
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     }
     int launches = (b->totalMeshVerts > 0 ? 1 : 0) + (b->sdfs.empty() ? 0 : (b->sdfL.totalTris > 0 ? 3 : 2));
-    for (auto& c : b->classes) launches += c.numItems > 0 ? 1 : 0;
+    for (auto& c : b->classes) launches += c.numItems > 0 ? 2 : 0;
     b->launchesPerFrame = launches;
     return TFX_OK;
 }
@@ -304,61 +360,79 @@ static int snapshot_restore(Snapshot& sn, cudaStream_t s) {
     return TFX_OK;
 }
 
+// Mean time of `frames` launches of the frame graph (captured for the current shapes), after one
+// untimed launch.
+static int time_graph_frames(tfx_batch b, int frames, float* ms) {
+    if (int r = capture_graphs(b)) return r;
+    cudaStream_t s = b->ctx->stream;
+    cudaEvent_t e0, e1;
+    TFX_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
+    TFX_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+    int rc = TFX_OK;
+    if (cudaGraphLaunch(b->graph[0], s) != cudaSuccess || cudaEventRecord(e0, s) != cudaSuccess) rc = TFX_ERR_CUDA;
+    for (int f = 0; f < frames && rc == TFX_OK; ++f)
+        if (cudaGraphLaunch(b->graph[0], s) != cudaSuccess) rc = TFX_ERR_CUDA;
+    if (rc == TFX_OK && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        *ms = t / (float)frames;
+        int flag = 0;
+        cudaMemcpy(&flag, b->devErr, sizeof(int), cudaMemcpyDeviceToHost);
+        if (flag) rc = fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+    } else if (rc == TFX_OK) {
+        rc = cuda_fail(cudaGetLastError(), "tfx_batch: autotune frame");
+    } else {
+        rc = cuda_fail(cudaGetLastError(), "tfx_batch: autotune graph launch");
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+// Coordinate descent over the launch shapes, each candidate timed as whole frames of the graph
+// (the SDF branch overlaps the strand kernels, so a part cannot be timed alone): the SDF construct's
+// block size, then per class the vertices per lane, warps per block and resident blocks per SM.
 static int autotune(tfx_batch b, int frames) {
     cudaStream_t s = b->ctx->stream;
-    TFX_CUDA(cudaMemcpyAsync(b->devBlock, b->staging.data(), b->blockBytes, cudaMemcpyHostToDevice, s), "tfx_batch: upload");
+    for (int i = 0; i < 2; ++i) std::memcpy(b->pinned[i], b->staging.data(), b->blockBytes);
     Snapshot sn;
     if (int r = snapshot_take(b, sn, s)) return r;
-    std::vector<float> part;
-    // best time of each part over `frames` frames with the current shapes
-    auto time_frames = [&](float* sdfMs, std::vector<float>* classMs) -> int {
-        float bestSdf = 1e30f;
-        std::vector<float> best(b->classes.size(), 1e30f);
-        for (int f = 0; f < frames; ++f) {
-            if (int r = launch_frame_direct(b, s, &part)) return r;
-            bestSdf = std::min(bestSdf, part[0]);
-            size_t k = 1;
-            for (size_t c = 0; c < b->classes.size(); ++c)
-                if (b->classes[c].numItems > 0 && k < part.size()) best[c] = std::min(best[c], part[k++]);
-        }
-        *sdfMs = bestSdf;
-        *classMs = best;
-        return TFX_OK;
-    };
     int rc = TFX_OK;
+    float best = 1e30f;
+    if ((rc = time_graph_frames(b, frames, &best))) { snapshot_restore(sn, s); return rc; }
     if (!b->sdfs.empty() && b->sdfL.totalTris > 0) {
-        float bestMs = 1e30f;
         int bestThreads = b->sdfL.constructThreads;
         for (int th : {64, 128, 256}) {
+            if (th == bestThreads) continue;
             b->sdfL.constructThreads = th;
-            float sdfMs;
-            std::vector<float> cm;
-            if ((rc = time_frames(&sdfMs, &cm))) break;
-            if (sdfMs < bestMs) { bestMs = sdfMs; bestThreads = th; }
+            float ms;
+            if ((rc = time_graph_frames(b, frames, &ms))) break;
+            if (ms < best) { best = ms; bestThreads = th; }
         }
         b->sdfL.constructThreads = bestThreads;
     }
     for (size_t ci = 0; ci < b->classes.size() && rc == TFX_OK; ++ci) {
         BatchClass& c = b->classes[ci];
         if (c.numItems == 0) continue;
-        float bestMs = 1e30f;
-        int bestV = c.vpl, bestW = c.warps;
+        int bestV = c.vpl, bestW = c.warps, bestCap = c.perSMCap;
         for (int vpl : {1, 2, 4}) {
             if (!fused_config_valid(c.n, vpl)) continue;
             for (int warps : {4, 8}) {
-                c.vpl = vpl;
-                c.warps = warps;
-                if (fused_blocks_per_sm(c.n, vpl, warps) <= 0) continue;
-                if ((rc = size_class(b, c))) break;
-                float sdfMs;
-                std::vector<float> cm;
-                if ((rc = time_frames(&sdfMs, &cm))) break;
-                if (cm[ci] < bestMs) { bestMs = cm[ci]; bestV = vpl; bestW = warps; }
+                const int perSM = fused_blocks_per_sm(c.n, vpl, warps);
+                if (perSM <= 0) continue;
+                for (int cap = perSM; cap >= std::max(1, perSM - 1); --cap) {
+                    if (vpl == bestV && warps == bestW && (cap == perSM ? 0 : cap) == bestCap) continue;
+                    c.vpl = vpl; c.warps = warps; c.perSMCap = cap == perSM ? 0 : cap;
+                    if ((rc = size_class(b, c))) break;
+                    float ms;
+                    if ((rc = time_graph_frames(b, frames, &ms))) break;
+                    if (ms < best) { best = ms; bestV = vpl; bestW = warps; bestCap = c.perSMCap; }
+                }
+                if (rc) break;
             }
             if (rc) break;
         }
-        c.vpl = bestV;
-        c.warps = bestW;
+        c.vpl = bestV; c.warps = bestW; c.perSMCap = bestCap;
         if (rc == TFX_OK) rc = size_class(b, c);
     }
     int rr = snapshot_restore(sn, s);
@@ -414,6 +488,9 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
     b->devErr = (int*)p;
     TFX_CUDA(cudaMemset(b->devErr, 0, sizeof(int)), "tfx_batch: clear error flag");
     TFX_CUDA(cudaMallocHost((void**)&b->pinnedErr, 2 * sizeof(int)), "tfx_batch: pinned error flag");
+    TFX_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking), "tfx_batch: side stream");
+    TFX_CUDA(cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming), "cudaEventCreate");
+    TFX_CUDA(cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming), "cudaEventCreate");
     b->pinnedErr[0] = b->pinnedErr[1] = 0;
 
     std::vector<BatchObject> objs(nobj);

@@ -12,21 +12,24 @@
 //                           (triangle, cell) pair does the reference's distance and an atomicMin on the
 //                           FloatFlip3 word.  The pairs and the encoding are the reference's, so the grid
 //                           is bit-identical.
-//  * k_fused_strands      - the six simulation stages (TressFXSimulation.hlsl:609-1001) and the SDF
-//                           collision (TressFXSDFCollision.hlsl:531-595) of a group of guide strands
-//                           (32, or 16 at n = 64) in one pass.  Phase 0: bulk asynchronous copies
-//                           (cp.async.bulk on an mbarrier) bring the group's Pos / Prev / InitialPos /
-//                           Tangent / RestLength rows into shared memory while warp 0 blends each
-//                           strand's bone matrix.  Phase 1a (one lane per strand): strand-level data.
-//                           Phase 1b (one thread per vertex): integration + global shape, VSP, bind
-//                           pose.  Phase 2 (one lane per strand, one warp per iteration): the
-//                           local-shape sweeps as a wavefront (iteration k runs two vertices behind
-//                           iteration k-1, which is exactly the order in which the sequential sweeps
-//                           read and write).  Phase 3a (n/VPL lanes per strand): wind, length
-//                           constraints (warp shuffles), tangents, velocity clamp.  Phase 3b (flat over
-//                           guide and follow vertices): follow hairs, collision, and the single write
-//                           of every buffer.  Blocks are persistent over the strand groups of every
-//                           object of one vertices-per-strand class.
+//  * k_fused_strands      - the six simulation stages of the guide strands (TressFXSimulation.hlsl:
+//                           609-975) for a group of guide strands (32, or 16 at n = 64) in one
+//                           pass.  Phase 0: bulk asynchronous copies (cp.async.bulk on an mbarrier)
+//                           bring the group's Pos / Prev / InitialPos / Tangent / RestLength rows into
+//                           shared memory while warp 0 blends each strand's bone matrix.  Phase 1a
+//                           (one lane per strand): strand-level data.  Phase 1b (one thread per
+//                           vertex): integration + global shape, VSP, bind pose.  Phase 2 (one lane
+//                           per strand, one warp per iteration): the local-shape sweeps as a
+//                           wavefront (iteration k runs two vertices behind iteration k-1, which is
+//                           exactly the order in which the sequential sweeps read and write).
+//                           Phase 3a (n/VPL lanes per strand): wind, length constraints (warp
+//                           shuffles), tangents, velocity clamp.  Phase 3c: the guides' state is
+//                           written once.  Blocks are persistent over the strand groups of every
+//                           object of one vertices-per-strand class.  Needs no SDF, so it runs
+//                           while the frame's SDFs are being built.
+//  * k_follow_collide     - UpdateFollowHairVertices (TressFXSimulation.hlsl:978-1001) and the SDF
+//                           collision (TressFXSDFCollision.hlsl:531-595) of every guide and follow
+//                           vertex, after both.
 // All per-vertex arithmetic is the reference's, in the same order, so every buffer matches the
 // plain path and the oracle bit for bit.
 #include "tfx_batch.h"
@@ -509,74 +512,93 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
         }
         __syncthreads();
 
-        // ------------------------------------------------------------ phase 3b: follow hairs, collision, writes
-        // Flat over the group's (strand, hair, vertex) elements; element e of guide s is global vertex
-        // (gs0 + s*(F+1))*N + e%((F+1)*N): hair 0 is the guide, hairs 1..F its follows
-        // (UpdateFollowHairVertices, TressFXSimulation.hlsl:978-1001), every vertex then collided
-        // (CollideHairVerticesWithSdf_forward, TressFXSDFCollision.hlsl:531-595).  Four elements per
-        // thread are loaded before any is written, so their loads overlap.
-        {
-            const float* __restrict__ sdf = ob.sdf;
-            SdfGrid sg = SdfGrid{0.f, 0.f, 0.f, 1.f, 0, 0, 0, 0};
-            float margin = 0.0f;
-            if (sdf) { sg = ob.sdfFrame->grid; margin = ob.sdfFrame->margin; }
-            const float tip = c->tipSeparation;
-            const int rowLen = (F + 1) * N;
-            const int E = count * rowLen;
-            constexpr int U = 4;
-            for (int e0 = tid; e0 < E; e0 += U * nthreads) {
+        // ------------------------------------------------------------ phase 3c: write the guide state
+        // Pos / Prev / Tangent of the guides before collision; k_follow_collide adds the follow hairs
+        // and the collision once the frame's SDFs are built.
+        for (int e = tid; e < count * N; e += nthreads) {
+            const int s = e / N, j = e % N;
+            const int x = s * RS + j;
+            const size_t v = (size_t)(gs0 + s * (F + 1)) * N + j;
+            h.pos[v] = TP[x];
+            h.prev[v] = TV[x];
+            h.tan[v] = TT[x];
+        }
+        fence_proxy_async_smem();   // this group's shared-memory accesses come before the next group's copies
+        __syncthreads();
+    }
+}
+
+// ============================================================================================
+// follow hairs + collision
+//
+// UpdateFollowHairVertices (TressFXSimulation.hlsl:978-1001) and CollideHairVerticesWithSdf_forward
+// (TressFXSDFCollision.hlsl:531-595) for the groups of one vertices-per-strand class, after
+// k_fused_strands has written the guides' constrained state and the frame's SDFs are built.  One
+// thread per guide vertex; it makes the vertex's F follow vertices (hair i = 1..F) from the guide's
+// pre-collision position, then collides the guide vertex and every follow vertex.  The loads of U
+// hairs are issued before any of them is collided or written, so their latencies overlap.
+template <int N>
+__global__ void __launch_bounds__(256) k_follow_collide(const BatchObject* __restrict__ objs,
+                                                        const WorkItem* __restrict__ items, int numItems) {
+    constexpr int U = 4;
+    constexpr float kInvN = 1.0f / (float)N;   // exact: N is a power of two, so j * kInvN == j / N
+    for (int it = blockIdx.x; it < numItems; it += gridDim.x) {
+        const WorkItem wi = items[it];
+        const BatchObject& ob = objs[wi.obj];
+        const HairView h = ob.hair;
+        const int F = h.F;
+        const float* __restrict__ sdf = ob.sdf;
+        if (F == 0 && !sdf) continue;
+        SdfGrid sg = SdfGrid{0.f, 0.f, 0.f, 1.f, 0, 0, 0, 0};
+        float margin = 0.0f;
+        if (sdf) { sg = ob.sdfFrame->grid; margin = ob.sdfFrame->margin; }
+        const float tip = ob.consts->tipSeparation;
+        const int gs0 = wi.firstGuide * (F + 1);
+        for (int e = threadIdx.x; e < wi.count * N; e += blockDim.x) {
+            const int s = e / N, j = e % N;
+            const int gs = gs0 + s * (F + 1);
+            const size_t vg = (size_t)gs * N + j;
+            const float4 gp = h.pos[vg];
+            const float4 tn = h.tan[vg];
+            const bool collide = sdf && j >= 2;
+            const float factor = tip * ((float)j * kInvN) + 1.0f;
+            for (int i0 = 0; i0 <= F; i0 += U) {
                 float3 pt[U];
                 float wU[U], dist[U];
-                int vg[U], xs[U], jj[U], hh[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    const int e = e0 + u * nthreads;
-                    hh[u] = -1;
-                    if (e < E) {
-                        const int s = e / rowLen, r = e - s * rowLen;
-                        const int i = r / N, j = r % N;
-                        const int gs = gs0 + s * (F + 1);
-                        const int x = s * RS + j;
-                        hh[u] = i; jj[u] = j; xs[u] = x;
-                        vg[u] = gs * N + r;
-                        const float4 gp = TP[x];
-                        if (i == 0) {
-                            pt[u] = xyz(gp);
-                            wU[u] = gp.w;
-                        } else {
-                            const float4 off = __ldg(h.followOffset + gs + i);
-                            const float factor = tip * ((float)j / (float)N) + 1.0f;
-                            pt[u] = add(xyz(gp), mul(factor, xyz(off)));
-                            // inverse mass of the follow vertex: no thread writes this word before this read
-                            wU[u] = __ldg(&h.pos[vg[u]].w);
-                        }
+                    const int i = i0 + u;
+                    pt[u] = xyz(gp);
+                    wU[u] = gp.w;
+                    if (i > 0 && i <= F) {
+                        const float4 off = __ldg(h.followOffset + gs + i);
+                        pt[u] = add(xyz(gp), mul(factor, xyz(off)));
+                        // inverse mass of the follow vertex: only this thread writes the word, after this read
+                        wU[u] = __ldg(&h.pos[vg + (size_t)i * N].w);
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     dist[u] = 1e10f;
-                    if (hh[u] >= 0 && sdf && jj[u] >= 2) dist[u] = sdf_lookup(sdf, sg, pt[u]);
+                    if (collide && i0 + u <= F) dist[u] = sdf_lookup(sdf, sg, pt[u]);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
-                    if (hh[u] < 0) continue;
+                    const int i = i0 + u;
+                    if (i > F) continue;
+                    const size_t v = vg + (size_t)i * N;
                     float3 proj = pt[u];
-                    const bool hit = sdf && jj[u] >= 2 && sdf_collide_from(sdf, sg, margin, pt[u], dist[u], proj);
-                    const float3 fin = hit ? proj : pt[u];
-                    const int v = vg[u];
-                    h.pos[v] = make_float4(fin.x, fin.y, fin.z, wU[u]);
-                    h.tan[v] = TT[xs[u]];
-                    if (hh[u] == 0) {
-                        const float4 pv = TV[xs[u]];
-                        h.prev[v] = hit ? with_xyz(pv, proj) : pv;
+                    const bool hit = collide && sdf_collide_from(sdf, sg, margin, pt[u], dist[u], proj);
+                    if (i > 0) {
+                        h.pos[v] = make_float4(hit ? proj.x : pt[u].x, hit ? proj.y : pt[u].y, hit ? proj.z : pt[u].z, wU[u]);
+                        h.tan[v] = tn;
                     } else if (hit) {
-                        h.prev[v] = with_xyz(h.prev[v], proj);
+                        h.pos[v] = with_xyz(gp, proj);
                     }
+                    if (hit) h.prev[v] = with_xyz(h.prev[v], proj);
                 }
             }
         }
-        fence_proxy_async_smem();   // this group's shared-memory accesses come before the next group's copies
-        __syncthreads();
     }
 }
 
@@ -648,6 +670,38 @@ int fused_blocks_per_sm(int n, int vpl, int warps) {
     TFX_FUSED_OCC(64, 2)
     TFX_FUSED_OCC(64, 4)
     return 0;
+}
+
+template <int N>
+static cudaError_t launch_follow_n(const FollowLaunch& fl, cudaStream_t s) {
+    k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems);
+    return cudaGetLastError();
+}
+
+int follow_blocks_per_sm(int n) {
+    int nb = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (n) {
+        case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<4>, 256, 0); break;
+        case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<8>, 256, 0); break;
+        case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<16>, 256, 0); break;
+        case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<32>, 256, 0); break;
+        case 64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<64>, 256, 0); break;
+        default: break;
+    }
+    return e == cudaSuccess ? nb : 0;
+}
+
+cudaError_t launch_follow_collide(const FollowLaunch& fl, cudaStream_t s) {
+    if (fl.numItems <= 0) return cudaSuccess;
+    switch (fl.n) {
+        case 4: return launch_follow_n<4>(fl, s);
+        case 8: return launch_follow_n<8>(fl, s);
+        case 16: return launch_follow_n<16>(fl, s);
+        case 32: return launch_follow_n<32>(fl, s);
+        case 64: return launch_follow_n<64>(fl, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s) {
