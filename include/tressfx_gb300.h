@@ -283,6 +283,17 @@ int tfx_batch_build(tfx_batch batch, int reserved);
 /* Times the candidate launch shapes over `frames` frames each on the current inputs, restores every
  * state buffer, and recaptures the graphs with the fastest shapes. */
 int tfx_batch_autotune(tfx_batch batch, int frames);
+/* Launch choices of a built batch (no counterpart in the reference; results are identical for every
+ * value).  tfx_batch_autotune sets them too; setting one recaptures the frame graphs. */
+typedef enum tfx_batch_option {
+    TFX_BATCH_EXPANDED_GRIDS = 1,   /* collision lookups on a corner-expanded copy of an SDF (8 corners
+                                       per cell): 0 never, 1 always, 2 (default) for the SDFs whose
+                                       objects make at least 4 lookups per cell each frame          */
+    TFX_BATCH_OVERLAP_SDF = 2,      /* 1: the SDF build runs concurrently with the strand kernels    */
+    TFX_BATCH_SDF_BLOCK = 3         /* threads per block of the SDF construct: 64, 128 or 256         */
+} tfx_batch_option;
+int tfx_batch_set_option(tfx_batch batch, int option, int value);
+int tfx_batch_get_option(tfx_batch batch, int option, int* value);
 /* Per-frame inputs (copied when tfx_batch_run is called): the constant block of hair object
  * `index` (TressFXSimulationParams, bone matrices [0, num_bones)), and its local-shape
  * re-dispatch count (m_CPULocalShapeIterations, TressFXHairObject.cpp:402-411). */

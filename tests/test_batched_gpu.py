@@ -134,3 +134,25 @@ def test_batch_rejects_bad_use(ctx):
     assert e.value.status == A.TFX_ERR_MISMATCH
     b.close()
     h.close()
+
+
+@pytest.mark.parametrize("expanded,overlap", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_batched_options_bit_exact(ctx, expanded, overlap):
+    """Corner-expanded lookups and the overlapped SDF branch change nothing in the results."""
+    sc = scene_head(seed=23, num_guides=200, n=16, follows=2, triangles=2500, sdf_cells=40, frames=4)
+    gpu = BatchedPipeline(ctx, sc)
+    try:
+        gpu.batch.set_option(gpu.batch.EXPANDED_GRIDS, expanded)
+        gpu.batch.set_option(gpu.batch.OVERLAP_SDF, overlap)
+        gpu.batch.set_option(gpu.batch.SDF_BLOCK, 64)
+        assert (gpu.batch.get_option(gpu.batch.EXPANDED_GRIDS), gpu.batch.get_option(gpu.batch.OVERLAP_SDF)) == \
+            (expanded, overlap)
+        ora = OraclePipeline(sc)
+        for f in range(4):
+            fin = gpu.step(f)
+            ora.step(fin)
+        assert_same(gpu.hair[0], ora.hair[0], f"expanded={expanded} overlap={overlap}")
+        with pytest.raises(Exception):
+            gpu.batch.set_option(gpu.batch.SDF_BLOCK, 100)
+    finally:
+        gpu.close()

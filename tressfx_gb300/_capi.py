@@ -170,6 +170,8 @@ _PROTOS = {
     "tfx_batch_add_sdf": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "tfx_batch_add_hair": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_int)]),
     "tfx_batch_build": (C.c_int, [P, C.c_int]),
+    "tfx_batch_set_option": (C.c_int, [P, C.c_int, C.c_int]),
+    "tfx_batch_get_option": (C.c_int, [P, C.c_int, C.POINTER(C.c_int)]),
     "tfx_batch_autotune": (C.c_int, [P, C.c_int]),
     "tfx_batch_set_hair_constants": (C.c_int, [P, C.c_int, C.POINTER(SimParams), C.c_int, C.c_int]),
     "tfx_batch_set_sdf_frame": (C.c_int, [P, C.c_int, C.POINTER(SdfGrid), F32]),

@@ -338,6 +338,16 @@ class Batch:
     def build(self) -> None:
         check(A.lib().tfx_batch_build(self.handle, 0), "tfx_batch_build")
 
+    EXPANDED_GRIDS, OVERLAP_SDF, SDF_BLOCK = 1, 2, 3
+
+    def set_option(self, option: int, value: int) -> None:
+        check(A.lib().tfx_batch_set_option(self.handle, option, value), "tfx_batch_set_option")
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int()
+        check(A.lib().tfx_batch_get_option(self.handle, option, C.byref(v)), "tfx_batch_get_option")
+        return v.value
+
     def autotune(self, frames: int = 3) -> None:
         check(A.lib().tfx_batch_autotune(self.handle, frames), "tfx_batch_autotune")
 

@@ -19,6 +19,7 @@ struct BatchObject {
     HairView hair;                 // state buffers and counts of the hair object
     const DevSimConsts* consts;    // this frame's constants (inside the device frame block)
     const float* sdf;              // decoded SDF grid of the object's collision mesh, or null
+    const float4* sdf8;            // its corner-expanded copy (8 corners per cell), or null
     const SdfFrame* sdfFrame;      // this frame's grid + margin (inside the device frame block)
 };
 
@@ -45,6 +46,7 @@ struct BatchSdf {
     const float4* mesh;       // skinned {position, normal}[V]
     const uint32_t* indices;  // uint32[3T]
     uint32_t* words;          // the grid: FloatFlip3 words while built, floats after
+    float4* expanded;         // corner-expanded copy, 2 float4 per cell, or null when not kept
     const SdfFrame* frame;    // grid of this frame
     long long firstQuad;      // prefix over SDFs of ceil(cells / 4)
     long long numCells;       // X*Y*Z
@@ -73,6 +75,7 @@ struct SdfBatchLaunch {
     int totalTris;
     long long totalQuads;
     int constructThreads;
+    int expand;      // some SDF keeps a corner-expanded copy: run the expansion
 };
 
 cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s);

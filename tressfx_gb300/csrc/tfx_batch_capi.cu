@@ -62,6 +62,9 @@ struct tfx_batch_t {
 
     // device tables
     void* devArena = nullptr;
+    void* expandedArena = nullptr;   // corner-expanded copies of the SDF grids
+    int expandMode = 2;              // TFX_BATCH_EXPANDED_GRIDS: 0 never, 1 always, 2 where lookups >= 4 per cell
+    std::vector<float4*> sdfExpanded;   // per SDF: its slot in expandedArena
     BatchObject* objTable = nullptr;
     BatchMesh* meshTable = nullptr;
     BatchSdf* sdfTable = nullptr;
@@ -70,6 +73,7 @@ struct tfx_batch_t {
     SdfBatchLaunch sdfL{};
 
     cudaStream_t side = nullptr;             // second capture branch: mesh skinning + SDF build
+    bool overlap = true;                     // capture the SDF branch on `side`
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
     int* devErr = nullptr;      // fused kernel: a block gave up waiting for its bulk copies
     int* pinnedErr = nullptr;   // its copy at the end of each frame, one word per slot
@@ -106,6 +110,7 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
     if (b->side) cudaStreamDestroy(b->side);
     if (b->devBlock) cudaFree(b->devBlock);
     if (b->devArena) cudaFree(b->devArena);
+    if (b->expandedArena) cudaFree(b->expandedArena);
     for (auto& c : b->classes)
         if (c.items) cudaFree(c.items);
     for (auto h : b->hairs) context_release(h->ctx);
@@ -163,8 +168,8 @@ static void describe(tfx_batch b) {
     for (auto& c : b->classes)
         k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d;",
                       c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n));
-    k += snprintf(buf + k, sizeof(buf) - k, " SDF build %s the strand kernels;",
-                  b->side ? "concurrent with" : "before");
+    k += snprintf(buf + k, sizeof(buf) - k, " SDF build %s the strand kernels%s;",
+                  b->overlap ? "concurrent with" : "before", b->sdfL.expand ? ", lookups on corner-expanded grids" : "");
     b->description = buf;
 }
 
@@ -271,7 +276,7 @@ static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* 
 // The frame body as captured into the graph: the SDF branch (mesh skinning + SDF build) on the side
 // stream runs concurrently with the strand kernels, which need no SDF; k_follow_collide waits for both.
 static int launch_frame_forked(tfx_batch b, cudaStream_t s) {
-    const bool fork = b->side && !b->sdfs.empty();
+    const bool fork = b->overlap && b->side && !b->sdfs.empty();
     if (fork) {
         TFX_CUDA(cudaEventRecord(b->evFork, s), "tfx_batch: fork");
         TFX_CUDA(cudaStreamWaitEvent(b->side, b->evFork, 0), "tfx_batch: fork");
@@ -311,7 +316,8 @@ static int capture_graphs(tfx_batch b) {
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     }
-    int launches = (b->totalMeshVerts > 0 ? 1 : 0) + (b->sdfs.empty() ? 0 : (b->sdfL.totalTris > 0 ? 3 : 2));
+    int launches = (b->totalMeshVerts > 0 ? 1 : 0) +
+                   (b->sdfs.empty() ? 0 : (b->sdfL.totalTris > 0 ? 3 : 2) + (b->sdfL.expand ? 1 : 0));
     for (auto& c : b->classes) launches += c.numItems > 0 ? 2 : 0;
     b->launchesPerFrame = launches;
     return TFX_OK;
@@ -360,33 +366,36 @@ static int snapshot_restore(Snapshot& sn, cudaStream_t s) {
     return TFX_OK;
 }
 
-// Mean time of `frames` launches of the frame graph (captured for the current shapes), after one
-// untimed launch.
+// Time per frame of the frame graph captured for the current shapes: the graph is uploaded and
+// launched twice untimed, then the mean over max(frames, 6) launches is taken twice and the smaller
+// kept (a freshly instantiated graph's first launches carry one-off costs).
 static int time_graph_frames(tfx_batch b, int frames, float* ms) {
     if (int r = capture_graphs(b)) return r;
     cudaStream_t s = b->ctx->stream;
+    const int n = std::max(frames, 6);
     cudaEvent_t e0, e1;
     TFX_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
     TFX_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
-    int rc = TFX_OK;
-    if (cudaGraphLaunch(b->graph[0], s) != cudaSuccess || cudaEventRecord(e0, s) != cudaSuccess) rc = TFX_ERR_CUDA;
-    for (int f = 0; f < frames && rc == TFX_OK; ++f)
-        if (cudaGraphLaunch(b->graph[0], s) != cudaSuccess) rc = TFX_ERR_CUDA;
-    if (rc == TFX_OK && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess) {
+    cudaError_t e = cudaGraphUpload(b->graph[0], s);
+    for (int w = 0; w < 2 && e == cudaSuccess; ++w) e = cudaGraphLaunch(b->graph[0], s);
+    float best = 1e30f;
+    for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+        e = cudaEventRecord(e0, s);
+        for (int f = 0; f < n && e == cudaSuccess; ++f) e = cudaGraphLaunch(b->graph[0], s);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         float t = 0.f;
-        cudaEventElapsedTime(&t, e0, e1);
-        *ms = t / (float)frames;
-        int flag = 0;
-        cudaMemcpy(&flag, b->devErr, sizeof(int), cudaMemcpyDeviceToHost);
-        if (flag) rc = fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
-    } else if (rc == TFX_OK) {
-        rc = cuda_fail(cudaGetLastError(), "tfx_batch: autotune frame");
-    } else {
-        rc = cuda_fail(cudaGetLastError(), "tfx_batch: autotune graph launch");
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (e == cudaSuccess) best = std::min(best, t / (float)n);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: autotune frames");
+    int flag = 0;
+    TFX_CUDA(cudaMemcpy(&flag, b->devErr, sizeof(int), cudaMemcpyDeviceToHost), "tfx_batch: error flag");
+    if (flag) return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+    *ms = best;
+    return TFX_OK;
 }
 
 // Coordinate descent over the launch shapes, each candidate timed as whole frames of the graph
@@ -437,6 +446,38 @@ static int autotune(tfx_batch b, int frames) {
     }
     int rr = snapshot_restore(sn, s);
     return rc ? rc : rr;
+}
+
+// Which SDFs keep a corner-expanded copy: none, all, or (mode 2) those whose objects make at least
+// four lookups per grid cell each frame (every vertex with j >= 2 is looked up at least once), where
+// one 32-byte record per lookup beats eight scattered words by more than the copy costs.
+static int apply_expand_mode(tfx_batch b) {
+    const int nsdf = (int)b->sdfs.size(), nobj = (int)b->hairs.size();
+    std::vector<double> lookups(nsdf, 0.0);
+    for (int o = 0; o < nobj; ++o)
+        if (b->hairSdf[o] >= 0) {
+            tfx_hair h = b->hairs[o];
+            lookups[b->hairSdf[o]] += (double)h->G * (h->F + 1) * (h->n - 2);
+        }
+    std::vector<BatchSdf> sdfs(nsdf);
+    std::vector<BatchObject> objs(nobj);
+    if (nsdf) TFX_CUDA(cudaMemcpy(sdfs.data(), b->sdfTable, sizeof(BatchSdf) * nsdf, cudaMemcpyDeviceToHost), "tfx_batch: SDFs");
+    TFX_CUDA(cudaMemcpy(objs.data(), b->objTable, sizeof(BatchObject) * nobj, cudaMemcpyDeviceToHost), "tfx_batch: objects");
+    int any = 0;
+    for (int i = 0; i < nsdf; ++i) {
+        const double cells = (double)b->sdfDims[3 * i] * b->sdfDims[3 * i + 1] * b->sdfDims[3 * i + 2];
+        const bool on = b->expandMode == 1 || (b->expandMode == 2 && lookups[i] >= 4.0 * cells);
+        sdfs[i].expanded = on ? b->sdfExpanded[i] : nullptr;
+        any |= on ? 1 : 0;
+    }
+    for (int o = 0; o < nobj; ++o) {
+        const int si = b->hairSdf[o];
+        objs[o].sdf8 = si >= 0 ? sdfs[si].expanded : nullptr;
+    }
+    if (nsdf) TFX_CUDA(cudaMemcpy(b->sdfTable, sdfs.data(), sizeof(BatchSdf) * nsdf, cudaMemcpyHostToDevice), "tfx_batch: SDFs");
+    TFX_CUDA(cudaMemcpy(b->objTable, objs.data(), sizeof(BatchObject) * nobj, cudaMemcpyHostToDevice), "tfx_batch: objects");
+    b->sdfL.expand = any;
+    return TFX_OK;
 }
 
 extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
@@ -493,6 +534,18 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
     TFX_CUDA(cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming), "cudaEventCreate");
     b->pinnedErr[0] = b->pinnedErr[1] = 0;
 
+    // corner-expanded grids: 8 floats per cell, at the SDF's quad prefix
+    std::vector<long long> sdfFirstQuad(nsdf, 0);
+    long long quadsTotal = 0;
+    for (int i = 0; i < nsdf; ++i) {
+        sdfFirstQuad[i] = quadsTotal;
+        quadsTotal += ((long long)b->sdfDims[3 * i] * b->sdfDims[3 * i + 1] * b->sdfDims[3 * i + 2] + 3) / 4;
+    }
+    if (nsdf > 0)
+        TFX_CUDA(cudaMalloc(&b->expandedArena, (size_t)quadsTotal * 4 * 32), "tfx_batch: corner-expanded grids");
+    b->sdfExpanded.assign(nsdf, nullptr);
+    for (int i = 0; i < nsdf; ++i) b->sdfExpanded[i] = reinterpret_cast<float4*>(b->expandedArena) + 2 * 4 * sdfFirstQuad[i];
+
     std::vector<BatchObject> objs(nobj);
     for (int o = 0; o < nobj; ++o) {
         tfx_hair h = b->hairs[o];
@@ -501,6 +554,7 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         const int si = b->hairSdf[o];
         objs[o].sdf = si >= 0 ? reinterpret_cast<const float*>(b->sdfs[si]->grid) : nullptr;
         objs[o].sdfFrame = si >= 0 ? reinterpret_cast<const SdfFrame*>(b->devBlock + b->sdfOff[si]) : nullptr;
+        objs[o].sdf8 = nullptr;   // set by apply_expand_mode
     }
     TFX_CUDA(cudaMemcpy(b->objTable, objs.data(), sizeof(BatchObject) * nobj, cudaMemcpyHostToDevice), "tfx_batch: objects");
 
@@ -534,13 +588,16 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         d.frame = reinterpret_cast<const SdfFrame*>(b->devBlock + b->sdfOff[i]);
         d.numCells = (long long)b->sdfDims[3 * i] * b->sdfDims[3 * i + 1] * b->sdfDims[3 * i + 2];
         d.firstQuad = firstQuad;
+        d.expanded = nullptr;     // set by apply_expand_mode
         d.firstTriangle = firstTri;
         firstQuad += (d.numCells + 3) / 4;
         firstTri += d.numTriangles;
     }
     if (nsdf > 0)
         TFX_CUDA(cudaMemcpy(b->sdfTable, sdfs.data(), sizeof(BatchSdf) * nsdf, cudaMemcpyHostToDevice), "tfx_batch: SDFs");
-    b->sdfL = SdfBatchLaunch{b->sdfTable, nsdf, firstTri, firstQuad, 128};
+    b->sdfL = SdfBatchLaunch{b->sdfTable, nsdf, firstTri, firstQuad, 128, 0};
+    b->expandMode = 2;
+    if (int r = apply_expand_mode(b)) return r;
 
     // ---- strand classes (one fused launch per vertices-per-strand count present)
     for (int n : {4, 8, 16, 32, 64}) {
@@ -673,6 +730,44 @@ extern "C" int tfx_batch_profile_frame(tfx_batch b, float* part_ms, int max_part
     for (int i = 0; i < k; ++i)
         if (part_ms) part_ms[i] = part[i];
     *num_parts = (int)part.size();
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_set_option(tfx_batch b, int option, int value) {
+    if (!b || !b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: batch not built");
+    switch (option) {
+        case TFX_BATCH_EXPANDED_GRIDS:
+            if (value < 0 || value > 2) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: expanded grids %d", value);
+            TFX_CUDA(cudaStreamSynchronize(b->ctx->stream), "cudaStreamSynchronize");
+            b->expandMode = value;
+            if (int r = apply_expand_mode(b)) return r;
+            break;
+        case TFX_BATCH_OVERLAP_SDF:
+            if (value != 0 && value != 1) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: overlap %d", value);
+            b->overlap = value != 0;
+            break;
+        case TFX_BATCH_SDF_BLOCK:
+            if (value != 64 && value != 128 && value != 256)
+                return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: SDF block %d (64, 128 or 256)", value);
+            b->sdfL.constructThreads = value;
+            break;
+        default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: unknown option %d", option);
+    }
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    TFX_CUDA(cudaStreamSynchronize(b->ctx->stream), "cudaStreamSynchronize");
+    if (int r = capture_graphs(b)) return r;
+    describe(b);
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_get_option(tfx_batch b, int option, int* value) {
+    if (!b || !value) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_get_option: null argument");
+    switch (option) {
+        case TFX_BATCH_EXPANDED_GRIDS: *value = b->expandMode; break;
+        case TFX_BATCH_OVERLAP_SDF: *value = b->overlap ? 1 : 0; break;
+        case TFX_BATCH_SDF_BLOCK: *value = b->sdfL.constructThreads; break;
+        default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_get_option: unknown option %d", option);
+    }
     return TFX_OK;
 }
 

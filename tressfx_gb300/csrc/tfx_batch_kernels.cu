@@ -114,6 +114,31 @@ __global__ void __launch_bounds__(256) k_batch_sdf_finalize(const BatchSdf* __re
     }
 }
 
+// Corner-expanded copy of a finalized grid: record c holds the eight corners a trilinear lookup in
+// cell c reads, in TrilinearInterpolate's order ((x,y,z), (x+1,y,z), (x,y+1,z), (x+1,y+1,z), then the
+// same at z+1), so a lookup reads one 32-byte record instead of eight scattered words.  Only the
+// cells a lookup can use (x < nx-1, y < ny-1, z < nz-1) are written.
+__global__ void __launch_bounds__(256) k_batch_sdf_expand(const BatchSdf* __restrict__ sdfs, int nsdf,
+                                                          long long totalQuads) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4 * totalQuads; t += stride) {
+        const BatchSdf& s = sdfs[find_by_prefix_quad(sdfs, nsdf, t >> 2)];
+        const long long c = t - 4 * s.firstQuad;
+        if (c >= s.numCells || !s.expanded) continue;
+        const SdfGrid g = s.frame->grid;
+        const long long nxy = (long long)g.nx * g.ny;
+        const int z = (int)(c / nxy);
+        const long long r = c - (long long)z * nxy;
+        const int y = (int)(r / g.nx), x = (int)(r - (long long)y * g.nx);
+        if (x >= g.nx - 1 || y >= g.ny - 1 || z >= g.nz - 1) continue;
+        const float* f = reinterpret_cast<const float*>(s.words);
+        const long long Y = g.nx, Z = nxy;
+        float4* o = s.expanded + 2 * c;
+        o[0] = make_float4(f[c], f[c + 1], f[c + Y], f[c + Y + 1]);
+        o[1] = make_float4(f[c + Z], f[c + Z + 1], f[c + Z + Y], f[c + Z + Y + 1]);
+    }
+}
+
 // ConstructSignedDistanceField, :329-397, one warp per triangle.
 __global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __restrict__ sdfs, int nsdf, int totalTris) {
     const int warpsTotal = gridDim.x * (blockDim.x >> 5);
@@ -128,10 +153,26 @@ __global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __r
         int3 lo, hi;
         tri_cell_box(g, x0, x1, x2, lo, hi);
         const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
-        const int vol = nx * ny * nz;
+        const int nxy = nx * ny;
+        const int vol = nxy * nz;
         const TriPre P = tri_pre(x0, x1, x2);
+        // Box coordinates of c.  (c + 0.5) / m lies at least 0.5 / m from an integer, and the float
+        // product (c + 0.5) * (1 / m) is within (c / m) * 2^-23 of it, so its truncation is the
+        // integer quotient while c < 2^22; larger boxes use integer division.
+        const bool floatIdx = vol < (1 << 22);
+        const float inxy = 1.0f / (float)nxy, inx = 1.0f / (float)nx;
         for (int c = lane; c < vol; c += 32) {
-            const int x = lo.x + c % nx, y = lo.y + (c / nx) % ny, z = lo.z + c / (nx * ny);
+            int cz, r, cy;
+            if (floatIdx) {
+                cz = (int)(((float)c + 0.5f) * inxy);
+                r = c - cz * nxy;
+                cy = (int)(((float)r + 0.5f) * inx);
+            } else {
+                cz = c / nxy;
+                r = c - cz * nxy;
+                cy = r / nx;
+            }
+            const int x = lo.x + (r - cy * nx), y = lo.y + cy, z = lo.z + cz;
             const float d = signed_dist_pre(sdf_cell_pos(g, x, y, z), P);
             atomicMin(s.words + ((long long)z * g.ny + y) * g.nx + x, float_flip3(d));
         }
@@ -528,6 +569,42 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
     }
 }
 
+// GetSignedDistance + TrilinearInterpolate (TressFXSDFCollision.hlsl:414-527) on the corner-expanded
+// grid: the same cell, bounds test, corner values and interpolation as sdf_lookup.
+__device__ __forceinline__ float sdf_lookup8(const float4* __restrict__ sdf8, const SdfGrid& g, float3 p) {
+    const int3 gc = sdf_coords(g, p);
+    if (!(0 <= gc.x && gc.x < g.nx - 2) || !(0 <= gc.y && gc.y < g.ny - 2) || !(0 <= gc.z && gc.z < g.nz - 2))
+        return 1e10f;
+    const long long base = ((long long)g.ny * g.nx) * gc.z + (long long)g.nx * gc.y + gc.x;
+    const float4 lo = __ldg(sdf8 + 2 * base), hi = __ldg(sdf8 + 2 * base + 1);
+    const float d[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (d[j] == 1e10f) return 1e10f;
+    const float3 cp = sdf_cell_pos(g, gc.x, gc.y, gc.z);
+    const float3 ip = divs(sub(p, cp), g.cell);
+    const float b0 = lerp_ref(lerp_ref(d[0], d[1], ip.x), lerp_ref(d[2], d[3], ip.x), ip.y);
+    const float b1 = lerp_ref(lerp_ref(d[4], d[5], ip.x), lerp_ref(d[6], d[7], ip.x), ip.y);
+    return lerp_ref(b0, b1, ip.z);
+}
+
+// sdf_collide_from with every lookup on the expanded grid.
+__device__ __forceinline__ bool sdf_collide_from8(const float4* __restrict__ sdf8, const SdfGrid& g, float margin,
+                                                  float3 p, float distance, float3& proj) {
+    if (distance > margin) return false;
+    const float h = 0.1f * g.cell;
+    const float fx = sdf_lookup8(sdf8, g, add(p, mul(mk3(1.0f, 0.0f, 0.0f), h)));
+    const float fy = sdf_lookup8(sdf8, g, add(p, mul(mk3(0.0f, 1.0f, 0.0f), h)));
+    const float fz = sdf_lookup8(sdf8, g, add(p, mul(mk3(0.0f, 0.0f, 1.0f), h)));
+    const float3 grad = mk3((fx - distance) / h, (fy - distance) / h, (fz - distance) / h);
+    const float3 nrm = normalize(grad);
+    if (distance < margin) {
+        proj = add(p, mul(nrm, margin - distance));
+        return true;
+    }
+    return false;
+}
+
 // ============================================================================================
 // follow hairs + collision
 //
@@ -548,6 +625,7 @@ __global__ void __launch_bounds__(256) k_follow_collide(const BatchObject* __res
         const HairView h = ob.hair;
         const int F = h.F;
         const float* __restrict__ sdf = ob.sdf;
+        const float4* __restrict__ sdf8 = ob.sdf8;
         if (F == 0 && !sdf) continue;
         SdfGrid sg = SdfGrid{0.f, 0.f, 0.f, 1.f, 0, 0, 0, 0};
         float margin = 0.0f;
@@ -580,7 +658,7 @@ __global__ void __launch_bounds__(256) k_follow_collide(const BatchObject* __res
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     dist[u] = 1e10f;
-                    if (collide && i0 + u <= F) dist[u] = sdf_lookup(sdf, sg, pt[u]);
+                    if (collide && i0 + u <= F) dist[u] = sdf8 ? sdf_lookup8(sdf8, sg, pt[u]) : sdf_lookup(sdf, sg, pt[u]);
                 }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
@@ -588,7 +666,8 @@ __global__ void __launch_bounds__(256) k_follow_collide(const BatchObject* __res
                     if (i > F) continue;
                     const size_t v = vg + (size_t)i * N;
                     float3 proj = pt[u];
-                    const bool hit = collide && sdf_collide_from(sdf, sg, margin, pt[u], dist[u], proj);
+                    const bool hit = collide && (sdf8 ? sdf_collide_from8(sdf8, sg, margin, pt[u], dist[u], proj)
+                                                      : sdf_collide_from(sdf, sg, margin, pt[u], dist[u], proj));
                     if (i > 0) {
                         h.pos[v] = make_float4(hit ? proj.x : pt[u].x, hit ? proj.y : pt[u].y, hit ? proj.z : pt[u].z, wU[u]);
                         h.tan[v] = tn;
@@ -722,6 +801,10 @@ cudaError_t launch_batch_sdf(const SdfBatchLaunch& L, cudaStream_t s) {
             L.sdfs, L.nsdf, L.totalTris);
     }
     k_batch_sdf_finalize<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
+    if (L.expand) {
+        const unsigned ge = (unsigned)std::min<long long>((4 * q + 255) / 256, 152LL * 32);
+        k_batch_sdf_expand<<<ge, 256, 0, s>>>(L.sdfs, L.nsdf, q);
+    }
     return cudaGetLastError();
 }
 

@@ -95,31 +95,35 @@ __device__ __forceinline__ TriPre tri_pre(float3 x0, float3 x1, float3 x2) {
     return T;
 }
 
-// DistancePointToEdge(p, a, b) with x10 = b - a and dot(x10, x10) precomputed.
-__device__ __forceinline__ float dist_point_edge_pre(float3 p, float3 a, float3 b, float3 x10, float dd) {
+// Squared DistancePointToEdge(p, a, b) with x10 = b - a and dot(x10, x10) precomputed: the value
+// whose sqrtf the reference takes.
+__device__ __forceinline__ float edge_dist2_pre(float3 p, float3 a, float3 b, float3 x10, float dd) {
     float t = dot(sub(b, p), x10) / dd;
     t = fmaxf(0.0f, fminf(t, 1.0f));
     const float3 q = sub(p, add(mul(t, a), mul(1.0f - t, b)));
-    return length(q);
+    return dot(q, q);
 }
 
+// SignedDistancePointToTriangle with one square root: the reference takes sqrtf of the face
+// distance, or of each edge distance and then the minimum; sqrtf is correctly rounded and so
+// monotone, hence min(sqrtf(u), sqrtf(v)) == sqrtf(min(u, v)) and the result is the same float.
 __device__ __forceinline__ float signed_dist_pre(float3 p, const TriPre& T) {
-    float d;
     const float3 px2 = sub(p, T.x2);
     const float b = dot(T.x12n, px2) / T.l2;
     const float a = (dot(T.x02n, px2) - T.l1 * b) / T.l0;
     const float c = (1.0f - a) - b;
     const float tol = 1e-8f;
+    float d2;
     if (a >= -tol && b >= -tol && c >= -tol) {
         const float3 nn = sub(p, add(add(mul(a, T.x0), mul(b, T.x1)), mul(c, T.x2)));
-        d = length(nn);
+        d2 = dot(nn, nn);
     } else {
-        d = dist_point_edge_pre(p, T.x0, T.x1, T.e01, T.d01);
-        const float d12 = dist_point_edge_pre(p, T.x1, T.x2, T.e12, T.d12);
-        const float d02 = dist_point_edge_pre(p, T.x0, T.x2, T.e02, T.d02);
-        d = fminf(d, d12);
-        d = fminf(d, d02);
+        const float u01 = edge_dist2_pre(p, T.x0, T.x1, T.e01, T.d01);
+        const float u12 = edge_dist2_pre(p, T.x1, T.x2, T.e12, T.d12);
+        const float u02 = edge_dist2_pre(p, T.x0, T.x2, T.e02, T.d02);
+        d2 = fminf(fminf(u01, u12), u02);
     }
+    float d = sqrtf(d2);
     d = (dot(sub(p, T.x0), T.nTri) < 0.0f) ? -d : d;
     return d;
 }
