@@ -313,6 +313,55 @@ int tfx_batch_describe(tfx_batch batch, char* buf, size_t len, int32_t* launches
  * [1..] = the fused strand launch of each vertices-per-strand class present (ascending n). */
 int tfx_batch_profile_frame(tfx_batch batch, float* part_ms, int max_parts, int* num_parts);
 
+/* ---------------------------------------------------------------------------------- learned collision proxy */
+/* No counterpart in the reference.  A pose-conditioned neural SDF: an MLP (xyz with 16 Fourier
+ * frequencies + 3 pose angles -> 4 x 64 SiLU -> 1, BF16 weights, FP32 accumulation, tensor cores) that
+ * predicts the grid SDF's distance (in cells, truncated to +-band) and is trained on samples of grid
+ * SDFs built by this library at sampled poses.  At collision time it replaces the grid for vertices
+ * it places farther than margin + contact_slack_cells from the surface; the others (the contact band) are
+ * collided exactly on the grid, built only on the cells their lookups read. */
+typedef struct tfx_nsdf_t* tfx_nsdf;
+typedef struct tfx_nsdf_desc {
+    float box_min[3], box_max[3];   /* input normalisation box (world)                              */
+    float cell_size;                /* distance unit: grid cell (world)                              */
+    float band_cells;               /* targets truncated to +-band_cells                             */
+    float pose_scale;               /* network input = pose angle (radians) * pose_scale             */
+    float sphere_center[3];         /* sphere around the mesh: unset grid points outside it are far  */
+    float sphere_radius;
+    uint32_t seed;
+    int64_t max_samples;            /* training pool capacity                                        */
+    int64_t max_eval_samples;       /* evaluation pool capacity                                      */
+    float contact_slack_cells;      /* band = network distance below margin + slack cells (0: 1)      */
+} tfx_nsdf_desc;
+int tfx_nsdf_create(tfx_context ctx, const tfx_nsdf_desc* desc, tfx_nsdf* out);
+int tfx_nsdf_destroy(tfx_nsdf nsdf);
+/* One pose of training (pool 0) or evaluation (pool 1) data: skins `mesh` with the bone matrices,
+ * rebuilds `sdf` on `grid` from it, and appends `count` samples labelled by that grid (75% near the
+ * surface with normal offsets of sigma_cells cells, 25% uniform in the grid box).  sphere = centre xyz
+ * and radius of a sphere around the posed mesh (NULL: the descriptor's): grid points left unset that
+ * lie outside it are labelled far (+band), those inside it are left out. */
+int tfx_nsdf_add_samples(tfx_nsdf nsdf, int pool, tfx_mesh mesh, tfx_sdf sdf, const tfx_sdf_grid* grid,
+                         const float* bone_matrices, int num_bones, const float pose[3], const float sphere[4],
+                         int count, float sigma_cells);
+/* `steps` Adam steps on minibatches of `batch` (a multiple of 512) samples of pool 0; *mean_loss =
+ * mean squared error (cells^2) over the last tenth of the steps. */
+int tfx_nsdf_train(tfx_nsdf nsdf, int steps, int batch, float learning_rate, float* mean_loss);
+/* Network output (cells), target (cells) and weight of every sample of a pool, to host arrays. */
+int tfx_nsdf_evaluate(tfx_nsdf nsdf, int pool, float* pred_cells, float* target_cells, float* weight,
+                      int64_t max_count, int64_t* count);
+/* Distances (world units) at `count` DEVICE points (float4, xyz used) under `pose`. */
+int tfx_nsdf_query(tfx_nsdf nsdf, const void* points, int count, const float pose[3], float* out);
+/* CollideHairVerticesWithSdf_forward for every vertex of `hair` with the proxy in front of the grid:
+ * the band vertices are collided on `sdf` (mesh already bound and skinned for this frame), built on
+ * `grid` at their cells only.  band_count (optional, host) receives the band size and synchronizes. */
+int tfx_nsdf_collide(tfx_nsdf nsdf, tfx_hair hair, tfx_sdf sdf, const tfx_sdf_grid* grid, float margin_world,
+                     const float pose[3], int32_t* band_count);
+/* Master FP32 parameters (tfx_nsdf_get_info's num_params floats), e.g. to save or load a network. */
+int tfx_nsdf_get_params(tfx_nsdf nsdf, float* params, size_t count);
+int tfx_nsdf_set_params(tfx_nsdf nsdf, const float* params, size_t count);
+int tfx_nsdf_get_info(tfx_nsdf nsdf, int32_t* num_params, int64_t* train_samples, int64_t* eval_samples,
+                      int32_t* steps);
+
 #ifdef __cplusplus
 }
 #endif

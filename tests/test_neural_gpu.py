@@ -1,0 +1,89 @@
+"""The learned collision proxy on the GPU: the tensor-core forward pass against a NumPy forward pass,
+training on the method's own grid SDFs, and collision through the proxy against grid collision."""
+import math
+
+import numpy as np
+import pytest
+
+import nsdf_ref as R
+
+pytestmark = pytest.mark.gpu
+
+
+def test_query_matches_numpy_forward(ctx):
+    torch = pytest.importorskip("torch")
+    from tressfx_gb300.api import NeuralSDF
+    lo, hi = np.array([-0.2, 1.3, -0.25]), np.array([0.25, 1.8, 0.2])
+    nsdf = NeuralSDF(ctx, lo, hi, cell_size=0.004, pose_scale=1.0 / 0.7, seed=3, max_samples=512, max_eval_samples=0)
+    rng = np.random.default_rng(0)
+    p = nsdf.params()
+    nz = p != 0
+    p[nz] *= rng.uniform(0.5, 1.5, nz.sum()).astype(np.float32)
+    for a, b in ((R.P_B1, R.P_W2), (R.P_B2, R.P_W3), (R.P_B3, R.P_W4), (R.P_B4, R.P_W5)):
+        p[a:b] = rng.normal(0, 0.3, b - a)
+    p[R.P_B5] = 0.7
+    nsdf.set_params(p)
+    P = 3000
+    pts = rng.uniform(lo, hi, (P, 3)).astype(np.float32)
+    pose = (0.3, -0.45, 0.6)
+    dev = torch.zeros((P, 4), dtype=torch.float32, device="cuda")
+    dev[:, :3] = torch.from_numpy(pts).cuda()
+    out = torch.empty(P, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    nsdf.query_device(dev.data_ptr(), P, pose, out.data_ptr())
+    ctx.synchronize()
+    got = out.cpu().numpy() / np.float32(0.004)
+    want = R.forward(p, R.features(pts, pose, R.frame(lo, hi, 1.0 / 0.7)))
+    err = np.abs(got - want)
+    assert np.isfinite(got).all()
+    assert err.max() < 0.05 + 0.02 * np.abs(want).max(), (err.max(), np.abs(want).max())
+    assert np.median(err) < 0.01 + 0.005 * np.abs(want).max()
+    nsdf.close()
+
+
+@pytest.fixture(scope="module")
+def small_proxy(ctx):
+    from tressfx_gb300 import synthetic as S
+    from tressfx_gb300.neural import train_proxy
+    sc = S.scene_neural(num_guides=500, n=16, triangles=3000, sdf_cells=48, frames=12)
+    nsdf, rep = train_proxy(ctx, sc.objects[0], poses=96, samples_per_pose=4096, eval_poses=8,
+                            eval_samples_per_pose=4096, steps=1500, batch=4096, lr=2e-3, contact_slack_cells=2.0)
+    print("proxy:", rep)
+    yield sc, nsdf, rep
+    nsdf.close()
+
+
+def test_training_learns_the_grid_sdf(small_proxy):
+    _, _, rep = small_proxy
+    assert rep.samples == 96 * 4096 and rep.eval_points > 1000
+    assert math.isfinite(rep.final_loss) and rep.final_loss < 0.5
+    assert rep.error_mean_cells < 0.5, rep
+
+
+def test_collision_through_the_proxy_matches_the_grid(ctx, small_proxy):
+    """Vertices the network places outside the contact band are not collided; the band is collided
+    exactly on the grid.  With the network within the slack of the grid, every buffer equals the
+    grid-collided frames bit for bit, and the band is a strict subset of the vertices."""
+    from tressfx_gb300 import _capi as A
+    from tressfx_gb300.headless import NeuralPipeline, PlainPipeline
+    sc, nsdf, _ = small_proxy
+    a = PlainPipeline(ctx, sc)
+    b = NeuralPipeline(ctx, sc, nsdf)
+    try:
+        for f in range(10):
+            a.step(f)
+            fin = b.step(f) if f < 9 else None
+            if f == 9:
+                from tressfx_gb300.headless import FrameInputs
+                fin = FrameInputs(sc, f)
+                b.prepare(fin)
+                b.run(fin, record_band=True)
+        band = b.band_counts[-1]
+        total = b.hair[0].num_vertices
+        for buf in (A.BUF_POSITIONS, A.BUF_POSITIONS_PREV, A.BUF_TANGENTS):
+            x, y = a.hair[0].read(buf).view(np.uint32), b.hair[0].read(buf).view(np.uint32)
+            assert np.array_equal(x, y), f"buffer {buf}: {int((x != y).any(axis=1).sum())} vertices differ"
+        assert 0 < band < total
+    finally:
+        a.close()
+        b.close()

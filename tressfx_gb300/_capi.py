@@ -107,6 +107,13 @@ class SdfGrid(C.Structure):
         return self.num_cells_x * self.num_cells_y * self.num_cells_z
 
 
+class NsdfDesc(C.Structure):
+    _fields_ = [("box_min", C.c_float * 3), ("box_max", C.c_float * 3), ("cell_size", C.c_float),
+                ("band_cells", C.c_float), ("pose_scale", C.c_float), ("sphere_center", C.c_float * 3),
+                ("sphere_radius", C.c_float), ("seed", C.c_uint32), ("max_samples", C.c_int64),
+                ("max_eval_samples", C.c_int64), ("contact_slack_cells", C.c_float)]
+
+
 class TfxError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{status_name(status)}: {message}")
@@ -165,6 +172,17 @@ _PROTOS = {
     "tfx_mesh_skin": (C.c_int, [P, P, C.c_int]),
     "tfx_mesh_get_buffers": (C.c_int, [P, C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tfx_mesh_read_skinned": (C.c_int, [P, P, C.c_size_t]),
+    "tfx_nsdf_create": (C.c_int, [P, C.POINTER(NsdfDesc), C.POINTER(P)]),
+    "tfx_nsdf_destroy": (C.c_int, [P]),
+    "tfx_nsdf_add_samples": (C.c_int, [P, C.c_int, P, P, C.POINTER(SdfGrid), P, C.c_int, FP, FP, C.c_int, F32]),
+    "tfx_nsdf_train": (C.c_int, [P, C.c_int, C.c_int, F32, FP]),
+    "tfx_nsdf_evaluate": (C.c_int, [P, C.c_int, P, P, P, C.c_int64, C.POINTER(C.c_int64)]),
+    "tfx_nsdf_query": (C.c_int, [P, P, C.c_int, FP, P]),
+    "tfx_nsdf_collide": (C.c_int, [P, P, P, C.POINTER(SdfGrid), F32, FP, C.POINTER(C.c_int32)]),
+    "tfx_nsdf_get_params": (C.c_int, [P, P, C.c_size_t]),
+    "tfx_nsdf_set_params": (C.c_int, [P, P, C.c_size_t]),
+    "tfx_nsdf_get_info": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int32)]),
     "tfx_batch_create": (C.c_int, [P, C.POINTER(P)]),
     "tfx_batch_destroy": (C.c_int, [P]),
     "tfx_batch_add_sdf": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),

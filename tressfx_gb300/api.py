@@ -388,3 +388,85 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class NeuralSDF:
+    """tfx_nsdf: the learned collision proxy (pose-conditioned neural SDF) over the C ABI."""
+
+    def __init__(self, ctx: Context, box_min, box_max, cell_size: float, band_cells: float = 3.0,
+                 pose_scale: float = 1.0 / 0.7, sphere=None, seed: int = 1, max_samples: int = 1 << 20,
+                 max_eval_samples: int = 1 << 18, contact_slack_cells: float = 1.0):
+        self.ctx = ctx
+        d = A.NsdfDesc()
+        for k in range(3):
+            d.box_min[k], d.box_max[k] = float(box_min[k]), float(box_max[k])
+        d.cell_size, d.band_cells, d.pose_scale = float(cell_size), float(band_cells), float(pose_scale)
+        if sphere is not None:
+            d.sphere_center[0], d.sphere_center[1], d.sphere_center[2] = (float(x) for x in sphere[:3])
+            d.sphere_radius = float(sphere[3])
+        d.seed, d.max_samples, d.max_eval_samples = int(seed), int(max_samples), int(max_eval_samples)
+        d.contact_slack_cells = float(contact_slack_cells)
+        h = C.c_void_p()
+        check(A.lib().tfx_nsdf_create(ctx.handle, C.byref(d), C.byref(h)), "tfx_nsdf_create")
+        self.handle = h
+        self.cell_size = float(cell_size)
+
+    def add_samples(self, pool: int, mesh: CollisionMesh, sdf: SDFCollision, grid: A.SdfGrid, bones: np.ndarray,
+                    pose, count: int, sphere=None, sigma_cells: float = 1.5) -> None:
+        b = np.ascontiguousarray(bones, dtype=np.float32).reshape(-1, 16)
+        p = (C.c_float * 3)(*[float(x) for x in pose])
+        sp = (C.c_float * 4)(*[float(x) for x in sphere]) if sphere is not None else None
+        check(A.lib().tfx_nsdf_add_samples(self.handle, pool, mesh.handle, sdf.handle, C.byref(grid), ptr(b), len(b), p,
+                                           sp, int(count), float(sigma_cells)), "tfx_nsdf_add_samples")
+
+    def train(self, steps: int, batch: int = 8192, lr: float = 1e-3) -> float:
+        loss = C.c_float()
+        check(A.lib().tfx_nsdf_train(self.handle, int(steps), int(batch), float(lr), C.byref(loss)), "tfx_nsdf_train")
+        return float(loss.value)
+
+    def evaluate(self, pool: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        _, tr, ev, _ = self.info()
+        n = tr if pool == 0 else ev
+        pred, tgt, w = (np.empty(n, np.float32) for _ in range(3))
+        cnt = C.c_int64()
+        check(A.lib().tfx_nsdf_evaluate(self.handle, pool, ptr(pred), ptr(tgt), ptr(w), n, C.byref(cnt)),
+              "tfx_nsdf_evaluate")
+        return pred[:cnt.value], tgt[:cnt.value], w[:cnt.value]
+
+    def query_device(self, points_ptr: int, count: int, pose, out_ptr: int) -> None:
+        p = (C.c_float * 3)(*[float(x) for x in pose])
+        check(A.lib().tfx_nsdf_query(self.handle, points_ptr, int(count), p, out_ptr), "tfx_nsdf_query")
+
+    def collide(self, hair: HairObject, sdf: SDFCollision, grid: A.SdfGrid, margin_world: float, pose,
+                band: bool = False) -> int | None:
+        p = (C.c_float * 3)(*[float(x) for x in pose])
+        n = C.c_int32()
+        check(A.lib().tfx_nsdf_collide(self.handle, hair.handle, sdf.handle, C.byref(grid), float(margin_world), p,
+                                       C.byref(n) if band else None), "tfx_nsdf_collide")
+        return n.value if band else None
+
+    def params(self) -> np.ndarray:
+        n = self.info()[0]
+        out = np.empty(n, np.float32)
+        check(A.lib().tfx_nsdf_get_params(self.handle, ptr(out), n), "tfx_nsdf_get_params")
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(A.lib().tfx_nsdf_set_params(self.handle, ptr(p), len(p)), "tfx_nsdf_set_params")
+
+    def info(self) -> tuple[int, int, int, int]:
+        a, b, c, d = C.c_int32(), C.c_int64(), C.c_int64(), C.c_int32()
+        check(A.lib().tfx_nsdf_get_info(self.handle, C.byref(a), C.byref(b), C.byref(c), C.byref(d)), "tfx_nsdf_get_info")
+        return a.value, b.value, c.value, d.value
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            A.lib().tfx_nsdf_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -150,3 +150,27 @@ class BatchedPipeline(PlainPipeline):
     def close(self) -> None:
         self.batch.close()
         super().close()
+
+
+class NeuralPipeline(PlainPipeline):
+    """The plain path with the learned collision proxy in front of the grid: per frame the mesh is
+    skinned, the hair simulated, and tfx_nsdf_collide classifies every vertex with the network and
+    collides the contact band exactly on a grid built at the band's cells only."""
+
+    def __init__(self, ctx: Context, scene: Scene, proxy):
+        super().__init__(ctx, scene)
+        self.proxy = proxy
+        self.band_counts: list[int] = []
+
+    def run(self, fin: FrameInputs, record_band: bool = False) -> None:
+        for m, mb in zip(self.meshes, fin.mesh_bones):
+            if m is not None:
+                m.skin(mb)
+        self.sim.simulate(self.hair)
+        pose = self.scene.meta["pose_fn"](fin.frame * self.scene.dt)
+        for h, s, o, g in zip(self.hair, self.sdfs, self.scene.objects, fin.grids):
+            if s is not None:
+                n = self.proxy.collide(h, s, g, margin_world(o, g), pose, band=record_band)
+                if record_band:
+                    self.band_counts.append(n)
+        self.frame += 1

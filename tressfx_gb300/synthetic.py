@@ -389,6 +389,34 @@ def scene_head(seed: int = 2, num_guides: int = 20000, n: int = 32, follows: int
     return sc
 
 
+def pose_trajectory(seed: int = 9, amplitude_deg: float = 38.0):
+    """Smooth 3-joint pose (neck tilt, nod, turn) within +-amplitude: t -> angles (radians)."""
+    rng = np.random.default_rng(seed)
+    hz = rng.uniform(0.2, 0.6, 3)
+    ph = rng.uniform(0.0, 2.0 * math.pi, 3)
+    amp = math.radians(amplitude_deg)
+
+    def fn(t: float) -> np.ndarray:
+        return amp * np.sin(2.0 * math.pi * hz * t + ph)
+    return fn
+
+
+def scene_neural(seed: int = 9, num_guides: int = 20000, n: int = 32, triangles: int = 20000, sdf_cells: int = 128,
+                 frames: int = 300) -> Scene:
+    """The head scene's guides (no follow hairs) and mesh, driven by a 3-joint pose in +-40 degrees,
+    with a 128^3 grid: the workload of the learned collision proxy."""
+    sc = scene_head(seed=seed, num_guides=num_guides, n=n, follows=0, triangles=triangles, sdf_cells=sdf_cells,
+                    frames=frames)
+    traj = pose_trajectory(seed + 1)
+    obj = sc.objects[0]
+    bones = lambda t: pose_bones(NECK_PIVOT, traj(t))  # noqa: E731
+    obj.bone_fn = bones
+    obj.mesh_bone_fn = bones
+    sc.meta["pose_fn"] = traj
+    sc.name = f"neural_{num_guides}x{n}_sdf{sdf_cells}"
+    return sc
+
+
 def torso_mesh(triangles: int) -> Mesh:
     nl, nq = mesh_lat_lon_for(triangles)
     v, i = ellipsoid_mesh((0.0, 1.2, 0.0), (0.18, 0.3, 0.12), nl, nq)
