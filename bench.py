@@ -43,6 +43,8 @@ WORKLOADS = {
     "batched": "64 objects, strands log-uniform 512..50000 (x64 padded), n in {8,16,32,64}, SDF 32^3..128^3, "
                "5k..30k-tri meshes (24.2M verts)",
     "small": "plain small 2048x16, no SDF",
+    "neural": "learned collision proxy: head mesh (20k tris) posed by 3 joints in +-40 deg, 20000x32 guides, "
+              "MLP trained on 512 poses x 8192 samples of 128^3 grid SDFs",
 }
 
 
@@ -51,8 +53,9 @@ def load_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d.get("bf16_tflops", 1900.0)),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 class ClockSampler:
@@ -115,7 +118,8 @@ class ClockSampler:
 
 def make_scene(name: str):
     from tressfx_gb300 import synthetic as S
-    return {"head": S.scene_head, "fur": S.scene_fur, "small": S.scene_small, "batched": S.scene_batched}[name]()
+    return {"head": S.scene_head, "fur": S.scene_fur, "small": S.scene_small, "batched": S.scene_batched,
+            "neural": S.scene_neural}[name]()
 
 
 def plain_kernel_bytes(scene) -> dict[str, float]:
@@ -338,6 +342,101 @@ def run_reference(args) -> dict:
             "threads": threads}
 
 
+# ------------------------------------------------------------------------------------------ neural proxy
+MLP_FLOPS = 2 * (102 * 64 + 3 * 64 * 64 + 64)   # algorithmic flops of one query (unpadded layers)
+
+
+def run_neural(args, base_cfg: dict, metric: str) -> dict:
+    """The learned collision proxy on the head mesh under random poses: training (time, loss), distance
+    error against the 128^3 grids of held-out poses, query throughput, and frames of the plain path
+    with collision through the proxy against frames with grid collision (and whether they agree)."""
+    from tressfx_gb300 import _capi as A
+    from tressfx_gb300.api import Context
+    from tressfx_gb300.headless import FrameInputs, NeuralPipeline, PlainPipeline
+    from tressfx_gb300.neural import train_proxy
+    scene = make_scene("neural")
+    obj = scene.objects[0]
+    ctx = Context(0)
+    nsdf, rep = train_proxy(ctx, obj, poses=512, samples_per_pose=8192, eval_poses=64, eval_samples_per_pose=8192,
+                            steps=args.nsdf_steps, batch=8192, lr=3e-3, contact_slack_cells=2.0)
+    # ---- query throughput on the guide vertices (frame 0 state), CUDA events on the library's stream
+    grid_pipe = PlainPipeline(ctx, scene)
+    neural_pipe = NeuralPipeline(ctx, scene, nsdf)
+    h = grid_pipe.hair[0]
+    pos_ptr, _ = h.device_buffer(A.BUF_POSITIONS)
+    qn = h.num_vertices
+    from tressfx_gb300.api import SDFCollision
+    scratch = SDFCollision(ctx, qn)          # a device buffer of qn floats for the query output
+    import ctypes as C
+    qout = C.c_void_p()
+    assert A.lib().tfx_sdf_get_buffer(scratch.handle, C.byref(qout), None) == 0
+    pose = scene.meta["pose_fn"](0.0)
+    for _ in range(3):
+        nsdf.query_device(pos_ptr, qn, pose, qout.value)
+    ctx.synchronize()
+    ctx.timestamps()
+    ctx.timestamp("q0")
+    reps = 20
+    for _ in range(reps):
+        nsdf.query_device(pos_ptr, qn, pose, qout.value)
+    ctx.timestamp("q1")
+    st = ctx.timestamps()
+    q_ms = (st[-1][1] - st[0][1]) / reps
+    q_tflops = qn * MLP_FLOPS / (q_ms * 1e-3) / 1e12
+    # ---- frames: grid collision vs collision through the proxy, same inputs
+    inputs = [FrameInputs(scene, f) for f in range(args.warmup + args.steps)]
+
+    def timed(pipe, record=False):
+        for f in range(args.warmup):
+            pipe.prepare(inputs[f]); pipe.run(inputs[f])
+        ctx.synchronize(); ctx.timestamps(); ctx.timestamp("a")
+        for f in range(args.warmup, args.warmup + args.steps):
+            pipe.prepare(inputs[f]); pipe.run(inputs[f])
+        ctx.timestamp("b")
+        st = ctx.timestamps()
+        return (st[-1][1] - st[0][1]) / args.steps
+
+    g_ms = timed(grid_pipe)
+    n_ms = timed(neural_pipe)
+    # band size and agreement over a few more frames of both
+    bands = []
+    for f in range(args.steps, args.steps + 5):
+        fin = FrameInputs(scene, args.warmup + f)
+        grid_pipe.prepare(fin); grid_pipe.run(fin)
+        neural_pipe.prepare(fin); neural_pipe.run(fin, record_band=True)
+        bands.append(neural_pipe.band_counts[-1])
+    same = all(np.array_equal(grid_pipe.hair[0].read(b).view(np.uint32), neural_pipe.hair[0].read(b).view(np.uint32))
+               for b in (A.BUF_POSITIONS, A.BUF_POSITIONS_PREV, A.BUF_TANGENTS))
+    diff = int((grid_pipe.hair[0].read(A.BUF_POSITIONS) != neural_pipe.hair[0].read(A.BUF_POSITIONS)).any(axis=1).sum())
+    V = scene.vertices_per_frame
+    peaks = load_peaks()
+    line = {
+        "metric": metric, "value": V / (n_ms * 1e-3), "unit": "vertex-steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": n_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 simulation, bf16 proxy (f32 accumulate)", "data": "synthetic (seeded)",
+        "config": dict(base_cfg, path="plain path; collision: proxy classifies every vertex, contact band collided "
+                                      "exactly on a grid built at the band's cells"),
+        "grid_collision": {"value": V / (g_ms * 1e-3), "ms_per_step": g_ms},
+        "proxy": {"train_poses": rep.train_poses, "samples": rep.samples, "steps": rep.steps,
+                  "batch": 8192, "final_loss_cells2": rep.final_loss, "train_seconds": rep.train_seconds,
+                  "eval_poses": 64, "eval_points": rep.eval_points,
+                  "error_cells": {"mean": rep.error_mean_cells, "p99": rep.error_p99_cells, "max": rep.error_max_cells},
+                  "contact_slack_cells": 2.0,
+                  "band_fraction": float(np.mean(bands)) / V, "frames_equal_to_grid_collision": bool(same),
+                  "vertices_differing": diff},
+        "roofline": {"bound": "tensor", "kernel": "k_nsdf_query (mma.sync bf16)", "achieved": q_tflops,
+                     "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": q_tflops / peaks["bf16_tflops"],
+                     "traffic": None, "peak_source": peaks["source"], "queries": qn, "launch_ms": q_ms,
+                     "flops_per_query": MLP_FLOPS},
+    }
+    scratch.close()
+    neural_pipe.close()
+    grid_pipe.close()
+    nsdf.close()
+    ctx.close()
+    return line
+
+
 # ------------------------------------------------------------------------------------------ main
 def main() -> None:
     ap = argparse.ArgumentParser()
@@ -349,6 +448,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--autotune", type=int, default=2, help="frames per candidate shape (0: defaults)")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--nsdf-steps", type=int, default=6000, help="training steps of the proxy (--config neural)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -376,6 +476,13 @@ def main() -> None:
                     "e2e": {"value": r["value"], "unit": "vertex-steps/s", "h2d_bytes_per_step": 0,
                             "d2h_bytes_per_step": 0}}
             print(json.dumps(line), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    if args.config == "neural":
+        if rank == 0:
+            print(json.dumps(run_neural(args, base_cfg, metric)), flush=True)
         if dist is not None:
             dist.destroy_process_group()
         return

@@ -343,8 +343,9 @@ int tfx_nsdf_destroy(tfx_nsdf nsdf);
 int tfx_nsdf_add_samples(tfx_nsdf nsdf, int pool, tfx_mesh mesh, tfx_sdf sdf, const tfx_sdf_grid* grid,
                          const float* bone_matrices, int num_bones, const float pose[3], const float sphere[4],
                          int count, float sigma_cells);
-/* `steps` Adam steps on minibatches of `batch` (a multiple of 512) samples of pool 0; *mean_loss =
- * mean squared error (cells^2) over the last tenth of the steps. */
+/* `steps` Adam steps on minibatches of `batch` (a multiple of 512) samples of pool 0, the learning
+ * rate decaying from learning_rate to a tenth of it along a cosine; *mean_loss = mean squared error
+ * (cells^2) over the last tenth of the steps. */
 int tfx_nsdf_train(tfx_nsdf nsdf, int steps, int batch, float learning_rate, float* mean_loss);
 /* Network output (cells), target (cells) and weight of every sample of a pool, to host arrays. */
 int tfx_nsdf_evaluate(tfx_nsdf nsdf, int pool, float* pred_cells, float* target_cells, float* weight,

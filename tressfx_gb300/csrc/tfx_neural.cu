@@ -32,10 +32,31 @@ __device__ __forceinline__ void mma16816(float (&c)[4], uint32_t a0, uint32_t a1
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// The network is an approximation.  Its activation, SiLU(z) = z * sigmoid(z) = 0.5 z (1 + tanh(z / 2)),
+// is evaluated on bf16 pairs with the hardware tanh: one MUFU operation per two activations, and
+// the result is directly the next layer's bf16 A-fragment register.
+__device__ __forceinline__ uint32_t silu2(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(0.5f * a, 0.5f * b);
+    uint32_t t;
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<uint32_t*>(&h)));
+    const __nv_bfloat162 r = __hfma2(h, *reinterpret_cast<__nv_bfloat162*>(&t), h);
+    return *reinterpret_cast<const uint32_t*>(&r);
+}
+__device__ __forceinline__ float2 unpack_bf16(uint32_t u) {
+    return __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&u));
+}
 __device__ __forceinline__ float silu_grad(float z) {
-    const float s = 1.0f / (1.0f + __expf(-z));
+    const float s = __fdividef(1.0f, 1.0f + __expf(-z));
     return s * (1.0f + z * (1.0f - s));
+}
+
+// sin(pi x), cos(pi x): x reduced exactly to [-1, 1] (x - 2 * rint(x / 2) is exact in binary floating
+// point), then the hardware sine / cosine of pi * x'.
+__device__ __forceinline__ void sincospi_fast(float x, float* s, float* c) {
+    const float r = x - 2.0f * rintf(0.5f * x);
+    const float a = 3.14159265358979f * r;
+    *s = __sinf(a);
+    *c = __cosf(a);
 }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {   // lowbias32 (C. Wellons)
@@ -62,6 +83,17 @@ __device__ __forceinline__ void load_b(const __nv_bfloat16* W, int rs, int nt, i
     b0 = *reinterpret_cast<const uint32_t*>(r);
     b1 = *reinterpret_cast<const uint32_t*>(r + 8);
 }
+// B fragments of n-tiles nt and nt+1 (k-tile kt) with one ldmatrix.x4: lanes 8m..8m+7 address the rows
+// of 8x8 matrix m = (n-tile nt + m/2, k half m%2); rows are 16-byte aligned (row strides 144 / 240 B)
+// and the eight rows of a matrix fall in distinct bank quads.
+__device__ __forceinline__ void load_b2(const __nv_bfloat16* W, int rs, int nt, int kt, int lane, uint32_t (&b)[4]) {
+    const int m = lane >> 3, r = lane & 7;
+    const __nv_bfloat16* row = W + ((nt + (m >> 1)) * 8 + r) * rs + kt * 16 + (m & 1) * 8;
+    const uint32_t addr = (uint32_t)__cvta_generic_to_shared(row);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3])
+                 : "r"(addr));
+}
 // C fragments (8 n-tiles) initialised with a bias vector.
 __device__ __forceinline__ void init_bias(float (&C)[8][4], const float* b, int lane) {
     const int i = lane & 3;
@@ -71,21 +103,33 @@ __device__ __forceinline__ void init_bias(float (&C)[8][4], const float* b, int 
         C[nt][0] = b0; C[nt][1] = b1; C[nt][2] = b0; C[nt][3] = b1;
     }
 }
-// A fragments of the next layer from activations act(C).
+// A fragments of the next layer from C, through SiLU or as they are.
 template <bool SILU>
 __device__ __forceinline__ void c_to_a(const float (&C)[8][4], uint32_t (&A)[4][4]) {
 #pragma unroll
     for (int kt = 0; kt < 4; ++kt) {
-        float v[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            v[q] = SILU ? silu(C[2 * kt][q]) : C[2 * kt][q];
-            v[4 + q] = SILU ? silu(C[2 * kt + 1][q]) : C[2 * kt + 1][q];
+        if constexpr (SILU) {
+            A[kt][0] = silu2(C[2 * kt][0], C[2 * kt][1]);
+            A[kt][1] = silu2(C[2 * kt][2], C[2 * kt][3]);
+            A[kt][2] = silu2(C[2 * kt + 1][0], C[2 * kt + 1][1]);
+            A[kt][3] = silu2(C[2 * kt + 1][2], C[2 * kt + 1][3]);
+        } else {
+            A[kt][0] = pack_bf16(C[2 * kt][0], C[2 * kt][1]);
+            A[kt][1] = pack_bf16(C[2 * kt][2], C[2 * kt][3]);
+            A[kt][2] = pack_bf16(C[2 * kt + 1][0], C[2 * kt + 1][1]);
+            A[kt][3] = pack_bf16(C[2 * kt + 1][2], C[2 * kt + 1][3]);
         }
-        A[kt][0] = pack_bf16(v[0], v[1]);
-        A[kt][1] = pack_bf16(v[2], v[3]);
-        A[kt][2] = pack_bf16(v[4], v[5]);
-        A[kt][3] = pack_bf16(v[6], v[7]);
+    }
+}
+// The activations held in A fragments, back in C-fragment order (for storing them).
+__device__ __forceinline__ void a_to_c(const uint32_t (&A)[4][4], float (&H)[8][4]) {
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        float2 v;
+        v = unpack_bf16(A[kt][0]); H[2 * kt][0] = v.x; H[2 * kt][1] = v.y;
+        v = unpack_bf16(A[kt][1]); H[2 * kt][2] = v.x; H[2 * kt][3] = v.y;
+        v = unpack_bf16(A[kt][2]); H[2 * kt + 1][0] = v.x; H[2 * kt + 1][1] = v.y;
+        v = unpack_bf16(A[kt][3]); H[2 * kt + 1][2] = v.x; H[2 * kt + 1][3] = v.y;
     }
 }
 // C += A (16 x 64) * W^T for a 64-wide layer whose weights are stored [n][k] with row stride RSH.
@@ -93,10 +137,11 @@ __device__ __forceinline__ void layer64(float (&C)[8][4], const uint32_t (&A)[4]
 #pragma unroll
     for (int kt = 0; kt < 4; ++kt)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            uint32_t b0, b1;
-            load_b(W, RSH, nt, kt, lane, b0, b1);
-            mma16816(C[nt], A[kt][0], A[kt][1], A[kt][2], A[kt][3], b0, b1);
+        for (int nt = 0; nt < 8; nt += 2) {
+            uint32_t b[4];
+            load_b2(W, RSH, nt, kt, lane, b);
+            mma16816(C[nt], A[kt][0], A[kt][1], A[kt][2], A[kt][3], b[0], b[1]);
+            mma16816(C[nt + 1], A[kt][0], A[kt][1], A[kt][2], A[kt][3], b[2], b[3]);
         }
 }
 
@@ -113,15 +158,21 @@ __device__ __forceinline__ void write_features(__nv_bfloat16* F, int s, int half
         row[4] = __float2bfloat16(valid ? p1 : 0.f);
         row[5] = __float2bfloat16(valid ? p2 : 0.f);
     }
+    // f_{k+3} = 2 f_k: the three base frequencies of this half (k0, k0+1, k0+2) by the hardware sine /
+    // cosine, every later one by the double-angle formulas sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a
     const int k0 = half * (NFREQ / 2);
 #pragma unroll
-    for (int kk = 0; kk < NFREQ / 2; ++kk) {
-        const int k = k0 + kk;
+    for (int b = 0; b < 3; ++b) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             float sn = 0.f, cs = 0.f;
-            if (valid) sincospif(c_freq[k] * u[d], &sn, &cs);
-            *reinterpret_cast<__nv_bfloat162*>(row + 6 + 6 * k + 2 * d) = __floats2bfloat162_rn(sn, cs);
+            if (valid) sincospi_fast(c_freq[k0 + b] * u[d], &sn, &cs);
+#pragma unroll
+            for (int k = k0 + b; k < k0 + NFREQ / 2; k += 3) {
+                *reinterpret_cast<__nv_bfloat162*>(row + 6 + 6 * k + 2 * d) = __floats2bfloat162_rn(sn, cs);
+                const float s2 = 2.0f * sn * cs, c2 = 1.0f - 2.0f * sn * sn;
+                sn = s2; cs = c2;
+            }
         }
     }
     if (half == 1)
@@ -164,46 +215,41 @@ __device__ __forceinline__ void mlp_forward(const __nv_bfloat16* sW, const float
         uint32_t a[4];
         load_a(F, RS1, kt, lane, a);
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            uint32_t b0, b1;
-            load_b(sW + OFF_WT1, RS1, nt, kt, lane, b0, b1);
-            mma16816(C[nt], a[0], a[1], a[2], a[3], b0, b1);
+        for (int nt = 0; nt < 8; nt += 2) {
+            uint32_t b[4];
+            load_b2(sW + OFF_WT1, RS1, nt, kt, lane, b);
+            mma16816(C[nt], a[0], a[1], a[2], a[3], b[0], b[1]);
+            mma16816(C[nt + 1], a[0], a[1], a[2], a[3], b[2], b[3]);
         }
     }
     const int woff[3] = {OFF_WT2, OFF_WT3, OFF_WT4};
 #pragma unroll 1
     for (int l = 0; l < 3; ++l) {
         uint32_t A[4][4];
+        c_to_a<true>(C, A);
         if constexpr (TRAIN) {
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
                 for (int q = 0; q < 4; ++q) zsave[l * 32 + nt * 4 + q] = C[nt][q];
             float H[8][4];
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) H[nt][q] = silu(C[nt][q]);
+            a_to_c(A, H);
             store_pairs(H, 8, hout[l], HID, lane);
         }
-        c_to_a<true>(C, A);
         init_bias(C, sB + (l + 1) * HID, lane);
         layer64(C, A, sW + woff[l], lane);
     }
     uint32_t A[4][4];
+    c_to_a<true>(C, A);
     if constexpr (TRAIN) {
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int q = 0; q < 4; ++q) zsave[3 * 32 + nt * 4 + q] = C[nt][q];
         float H[8][4];
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) H[nt][q] = silu(C[nt][q]);
+        a_to_c(A, H);
         store_pairs(H, 8, hout[3], HID, lane);
     }
-    c_to_a<true>(C, A);
     float C5[4];
     {
         const int i = lane & 3;
@@ -220,6 +266,69 @@ __device__ __forceinline__ void mlp_forward(const __nv_bfloat16* sW, const float
     y1 = C5[2];
 }
 
+// Inference forward pass of a 32-point tile (two m-tiles sharing every weight fragment): rows
+// g, g+8 of tile 0 and g, g+8 of tile 1 come back in y[0..3] (valid in lanes with lane % 4 == 0).
+__device__ __forceinline__ void mlp_forward32(const __nv_bfloat16* sW, const float* sB, const __nv_bfloat16* F, int lane,
+                                              float (&y)[4]) {
+    float C[2][8][4];
+    init_bias(C[0], sB, lane);
+    init_bias(C[1], sB, lane);
+#pragma unroll 1
+    for (int kt = 0; kt < KIN / 16; ++kt) {
+        uint32_t a0[4], a1[4];
+        load_a(F, RS1, kt, lane, a0);
+        load_a(F + 16 * RS1, RS1, kt, lane, a1);
+#pragma unroll
+        for (int nt = 0; nt < 8; nt += 2) {
+            uint32_t b[4];
+            load_b2(sW + OFF_WT1, RS1, nt, kt, lane, b);
+            mma16816(C[0][nt], a0[0], a0[1], a0[2], a0[3], b[0], b[1]);
+            mma16816(C[1][nt], a1[0], a1[1], a1[2], a1[3], b[0], b[1]);
+            mma16816(C[0][nt + 1], a0[0], a0[1], a0[2], a0[3], b[2], b[3]);
+            mma16816(C[1][nt + 1], a1[0], a1[1], a1[2], a1[3], b[2], b[3]);
+        }
+    }
+    const int woff[3] = {OFF_WT2, OFF_WT3, OFF_WT4};
+#pragma unroll 1
+    for (int l = 0; l < 3; ++l) {
+        uint32_t A0[4][4], A1[4][4];
+        c_to_a<true>(C[0], A0);
+        c_to_a<true>(C[1], A1);
+        init_bias(C[0], sB + (l + 1) * HID, lane);
+        init_bias(C[1], sB + (l + 1) * HID, lane);
+        const __nv_bfloat16* W = sW + woff[l];
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt)
+#pragma unroll
+            for (int nt = 0; nt < 8; nt += 2) {
+                uint32_t b[4];
+                load_b2(W, RSH, nt, kt, lane, b);
+                mma16816(C[0][nt], A0[kt][0], A0[kt][1], A0[kt][2], A0[kt][3], b[0], b[1]);
+                mma16816(C[1][nt], A1[kt][0], A1[kt][1], A1[kt][2], A1[kt][3], b[0], b[1]);
+                mma16816(C[0][nt + 1], A0[kt][0], A0[kt][1], A0[kt][2], A0[kt][3], b[2], b[3]);
+                mma16816(C[1][nt + 1], A1[kt][0], A1[kt][1], A1[kt][2], A1[kt][3], b[2], b[3]);
+            }
+    }
+    uint32_t A0[4][4], A1[4][4];
+    c_to_a<true>(C[0], A0);
+    c_to_a<true>(C[1], A1);
+    float C5[2][4];
+    {
+        const int i = lane & 3;
+        const float b0 = sB[4 * HID + 2 * i], b1 = sB[4 * HID + 2 * i + 1];
+#pragma unroll
+        for (int t = 0; t < 2; ++t) { C5[t][0] = b0; C5[t][1] = b1; C5[t][2] = b0; C5[t][3] = b1; }
+    }
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+        uint32_t b0, b1;
+        load_b(sW + OFF_WT5, RSH, 0, kt, lane, b0, b1);
+        mma16816(C5[0], A0[kt][0], A0[kt][1], A0[kt][2], A0[kt][3], b0, b1);
+        mma16816(C5[1], A1[kt][0], A1[kt][1], A1[kt][2], A1[kt][3], b0, b1);
+    }
+    y[0] = C5[0][0]; y[1] = C5[0][2]; y[2] = C5[1][0]; y[3] = C5[1][2];
+}
+
 template <int WORDS>
 __device__ __forceinline__ void stage_weights(uint4* dst, const __nv_bfloat16* wbf, float* sB, const float* bias) {
     const uint4* src = reinterpret_cast<const uint4*>(wbf);
@@ -232,7 +341,7 @@ constexpr int ALL_U4 = WBF_ALL * 2 / 16;
 static_assert(WBF_FWD * 2 % 16 == 0 && WBF_ALL * 2 % 16 == 0, "weight blocks are copied as uint4");
 constexpr int TILE_BYTES = 16 * RS1 * 2;
 constexpr int QUERY_WARPS = 4;
-constexpr size_t QUERY_SMEM = (size_t)WBF_FWD * 2 + NBIAS * 4 + QUERY_WARPS * TILE_BYTES;
+constexpr size_t QUERY_SMEM = (size_t)WBF_FWD * 2 + NBIAS * 4 + QUERY_WARPS * 2 * TILE_BYTES;
 constexpr int TRAIN_WARPS = 4;
 constexpr size_t TRAIN_SMEM = (size_t)WBF_ALL * 2 + NBIAS * 4 + TRAIN_WARPS * (TILE_BYTES + 4 * 32 * 32 * 4);
 
@@ -247,13 +356,13 @@ __global__ void __launch_bounds__(QUERY_WARPS * 32) k_nsdf_query(const __nv_bflo
     __nv_bfloat16* sW = reinterpret_cast<__nv_bfloat16*>(smem_q);
     float* sB = reinterpret_cast<float*>(sW + WBF_FWD);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __nv_bfloat16* sF = reinterpret_cast<__nv_bfloat16*>(sB + NBIAS) + warp * 16 * RS1;
+    __nv_bfloat16* sF = reinterpret_cast<__nv_bfloat16*>(sB + NBIAS) + warp * 32 * RS1;
     stage_weights<FWD_U4>(smem_q, wbf, sB, bias);
     __syncthreads();
-    const int s = lane >> 1, half = lane & 1, g = lane >> 2, i = lane & 3;
+    const int g = lane >> 2, i = lane & 3;
     const int nw = gridDim.x * QUERY_WARPS;
-    for (int tile = blockIdx.x * QUERY_WARPS + warp; tile * 16 < count; tile += nw) {
-        const int idx = tile * 16 + s;
+    for (int tile = blockIdx.x * QUERY_WARPS + warp; tile * 32 < count; tile += nw) {
+        const int idx = tile * 32 + lane;
         const bool valid = idx < count;
         float px = 0.f, py = 0.f, pz = 0.f, a0 = pose.a0, a1 = pose.a1, a2 = pose.a2;
         if (valid) {
@@ -265,17 +374,20 @@ __global__ void __launch_bounds__(QUERY_WARPS * 32) k_nsdf_query(const __nv_bflo
                 px = P.x; py = P.y; pz = P.z;
             }
         }
-        write_features(sF, s, half, (px - fr.cx) * fr.ihx, (py - fr.cy) * fr.ihy, (pz - fr.cz) * fr.ihz,
-                       a0 * fr.poseScale, a1 * fr.poseScale, a2 * fr.poseScale, valid);
+        const float ux = (px - fr.cx) * fr.ihx, uy = (py - fr.cy) * fr.ihy, uz = (pz - fr.cz) * fr.ihz;
+        write_features(sF, lane, 0, ux, uy, uz, a0 * fr.poseScale, a1 * fr.poseScale, a2 * fr.poseScale, valid);
+        write_features(sF, lane, 1, ux, uy, uz, a0 * fr.poseScale, a1 * fr.poseScale, a2 * fr.poseScale, valid);
         __syncwarp();
-        float y0, y1;
-        mlp_forward<false>(sW, sB, sF, lane, nullptr, nullptr, y0, y1);
+        float y[4];
+        mlp_forward32(sW, sB, sF, lane, y);
         __syncwarp();
         if (i == 0) {
-            const int r0 = tile * 16 + g, r1 = r0 + 8;
             const float sc = SAMPLES ? 1.0f : fr.cell;
-            if (r0 < count) out[r0] = y0 * sc;
-            if (r1 < count) out[r1] = y1 * sc;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int row = tile * 32 + (r >> 1) * 16 + g + 8 * (r & 1);
+                if (row < count) out[row] = y[r] * sc;
+            }
         }
     }
 }
@@ -563,7 +675,7 @@ cudaError_t launch_query(const __nv_bfloat16* wbf, const float* bias, const Fram
     if (count <= 0) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_nsdf_query<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
-    const int tiles = (count + 15) / 16;
+    const int tiles = (count + 31) / 32;
     const int blocks = std::min((tiles + QUERY_WARPS - 1) / QUERY_WARPS, 152 * 8);
     k_nsdf_query<false><<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(wbf, bias, fr, points, nullptr, count, pose, out);
     return cudaGetLastError();
@@ -574,7 +686,7 @@ cudaError_t launch_query_samples(const __nv_bfloat16* wbf, const float* bias, co
     if (count <= 0) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_nsdf_query<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
-    const int tiles = (count + 15) / 16;
+    const int tiles = (count + 31) / 32;
     const int blocks = std::min((tiles + QUERY_WARPS - 1) / QUERY_WARPS, 152 * 8);
     k_nsdf_query<true><<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(wbf, bias, fr, nullptr, samples, count, Pose{0, 0, 0},
                                                                     out);
@@ -646,29 +758,30 @@ __global__ void __launch_bounds__(QUERY_WARPS * 32) k_nsdf_classify(CollideArgs 
     __nv_bfloat16* sW = reinterpret_cast<__nv_bfloat16*>(smem_c);
     float* sB = reinterpret_cast<float*>(sW + WBF_FWD);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __nv_bfloat16* sF = reinterpret_cast<__nv_bfloat16*>(sB + NBIAS) + warp * 16 * RS1;
+    __nv_bfloat16* sF = reinterpret_cast<__nv_bfloat16*>(sB + NBIAS) + warp * 32 * RS1;
     stage_weights<FWD_U4>(smem_c, a.wbf, sB, a.bias);
     __syncthreads();
     const Frame fr = a.fr;
-    const int s = lane >> 1, half = lane & 1, g = lane >> 2, i = lane & 3;
+    const int g = lane >> 2, i = lane & 3;
     const long long nw = (long long)gridDim.x * QUERY_WARPS;
     const float limit = a.margin / fr.cell + a.slackCells;   // band: network distance below margin + slack
-    for (long long tile = (long long)blockIdx.x * QUERY_WARPS + warp; tile * 16 < a.vtot; tile += nw) {
-        const long long v = tile * 16 + s;
+    for (long long tile = (long long)blockIdx.x * QUERY_WARPS + warp; tile * 32 < a.vtot; tile += nw) {
+        const long long v = tile * 32 + lane;
         const bool valid = v < a.vtot;
         const float4 P = valid ? a.pos[v] : make_float4(0.f, 0.f, 0.f, 0.f);
-        write_features(sF, s, half, (P.x - fr.cx) * fr.ihx, (P.y - fr.cy) * fr.ihy, (P.z - fr.cz) * fr.ihz,
-                       a.pose.a0 * fr.poseScale, a.pose.a1 * fr.poseScale, a.pose.a2 * fr.poseScale, valid);
+        const float ux = (P.x - fr.cx) * fr.ihx, uy = (P.y - fr.cy) * fr.ihy, uz = (P.z - fr.cz) * fr.ihz;
+        const float p0 = a.pose.a0 * fr.poseScale, p1 = a.pose.a1 * fr.poseScale, p2 = a.pose.a2 * fr.poseScale;
+        write_features(sF, lane, 0, ux, uy, uz, p0, p1, p2, valid);
+        write_features(sF, lane, 1, ux, uy, uz, p0, p1, p2, valid);
         __syncwarp();
-        float y0, y1;
-        mlp_forward<false>(sW, sB, sF, lane, nullptr, nullptr, y0, y1);
+        float y[4];
+        mlp_forward32(sW, sB, sF, lane, y);
         __syncwarp();
         if (i == 0) {
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const long long vr = tile * 16 + g + 8 * r;
-                const float y = r == 0 ? y0 : y1;
-                if (vr >= a.vtot || (int)(vr % a.n) < 2 || !(y < limit)) continue;
+            for (int r = 0; r < 4; ++r) {
+                const long long vr = tile * 32 + (r >> 1) * 16 + g + 8 * (r & 1);
+                if (vr >= a.vtot || (int)(vr % a.n) < 2 || !(y[r] < limit)) continue;
                 a.bandList[atomicAdd(a.bandCount, 1)] = (int)vr;
                 const float4 pv = a.pos[vr];
                 mark_block(a.marks, a.grid, sdf_coords(a.grid, mk3(pv.x, pv.y, pv.z)));
@@ -741,7 +854,7 @@ cudaError_t launch_collide(const CollideArgs& a, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaMemsetAsync(a.marks, 0, sizeof(uint32_t) * (size_t)((cells + 31) / 32), s);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nsdf_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
-    const long long tiles = (a.vtot + 15) / 16;
+    const long long tiles = (a.vtot + 31) / 32;
     const int blocks = (int)std::min<long long>((tiles + QUERY_WARPS - 1) / QUERY_WARPS, 152 * 8);
     k_nsdf_classify<<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(a);
     const unsigned gc = (unsigned)std::min<long long>((cells + 255) / 256, 152LL * 16);

@@ -170,7 +170,9 @@ extern "C" int tfx_nsdf_train(tfx_nsdf h, int steps, int batch, float lr, float*
         cudaError_t e = nsdf::launch_train_step(h->wbf, h->bias, h->fr, h->pool[0], h->poolSize[0], batch,
                                                 h->seed * 2654435761u + (uint32_t)h->step * 40503u, h->acts, h->grads,
                                                 h->lossSum, s);
-        if (e == cudaSuccess) e = nsdf::launch_adam(h->params, h->grads, h->m, h->v, h->step, lr, 1.0f, h->wbf, h->bias, s);
+        // cosine decay of the learning rate over this call's steps, to a tenth of it
+        const float lrk = lr * (0.1f + 0.45f * (1.0f + cosf(3.14159265f * (float)k / (float)steps)));
+        if (e == cudaSuccess) e = nsdf::launch_adam(h->params, h->grads, h->m, h->v, h->step, lrk, 1.0f, h->wbf, h->bias, s);
         if (e != cudaSuccess) return cuda_fail(e, "tfx_nsdf_train: step launch");
     }
     if (mean_loss) {
