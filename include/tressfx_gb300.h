@@ -197,6 +197,32 @@ int tfx_hair_get_buffer(tfx_hair hair, int buffer, void** device_ptr, size_t* by
  * (GetNumTotalHairVertices / Strands / VerticesPerStrand / FollowHairsPerGuideHair). */
 int tfx_hair_get_counts(tfx_hair hair, int32_t out[4]);
 
+/* ---------------------------------------------------------------------------------- strand quads */
+/* TressFXStrandParams (TressFXConstantBuffers.h) = cbuffer TressFXStrandParameters
+ * (TressFXRendering.hlsl:61-80). */
+typedef struct tfx_strand_params {
+    float mat_base_color[4];
+    float mat_tip_color[4];
+    float tip_percentage;
+    float strand_uv_tiling_factor;
+    float fiber_ratio;
+    float fiber_radius;
+    int32_t num_vertices_per_strand;
+    int32_t enable_thin_tip;
+    int32_t node_pool_size;
+    int32_t render_params_index;
+    int32_t enable_strand_uv;
+    int32_t enable_strand_tangent;
+    int32_t padding[2];
+} tfx_strand_params;
+/* GetExpandedTressFXVert (shadow = 0) or GetExpandedTressFXShadowVert (shadow = 1) of
+ * TressFXStrands.hlsl for every vertex id [0, 2 * Vtot) of the hair object, headless: out_device
+ * receives {Position, Tangent, p0p1, StrandColor} (4 float4) per id; the shadow form writes the
+ * position and zeros.  view_proj: 16 floats, row-major, applied as mul(M, v).  The root colour is
+ * mat_base_color (the albedo texture the shader samples is taken as white). */
+int tfx_hair_expand_strands(tfx_hair hair, const tfx_strand_params* params, const float eye[3], const float win_size[2],
+                            const float view_proj[16], int shadow, void* out_device);
+
 /* ---------------------------------------------------------------------------------- SDF */
 /* TressFXSDFCollisionParams (TressFXConstantBuffers.h:119-134), the grid part of it. */
 typedef struct tfx_sdf_grid {
@@ -230,6 +256,10 @@ int tfx_sdf_dispatch(tfx_sdf sdf, int kernel, const tfx_sdf_grid* grid);
 /* TressFXSDFCollision::CollideWithHair (TressFXSDFCollision.cpp:171-221): margin_world =
  * collisionMargin * cellSize (:194), applied to every vertex of the object. */
 int tfx_sdf_collide(tfx_sdf sdf, tfx_hair hair, const tfx_sdf_grid* grid, float margin_world);
+/* CollideHairVerticesWithSdf (TressFXSDFCollision.hlsl:599-715), the shader's faster variant that the
+ * reference's host code does not dispatch: every vertex (roots included), one 8-corner fetch, the
+ * gradient by forward or backward differences inside the same cell. */
+int tfx_sdf_collide_mixed(tfx_sdf sdf, tfx_hair hair, const tfx_sdf_grid* grid, float margin_world);
 int tfx_sdf_read(tfx_sdf sdf, void* host_dst, size_t bytes);
 int tfx_sdf_write(tfx_sdf sdf, const void* host_src, size_t bytes);
 int tfx_sdf_get_buffer(tfx_sdf sdf, void** device_ptr, size_t* bytes);

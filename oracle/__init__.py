@@ -53,6 +53,7 @@ def lib() -> C.CDLL:
         l.tfxo_ifloat_flip3.argtypes = [C.c_uint32]
         l.tfxo_ifloat_flip3.restype = C.c_uint32
         l.tfxo_mesh_skin_f32.argtypes = [vp, vp, vp, vp, i64, i32]
+        l.tfxo_sdf_collide_mixed_f32.argtypes = [vp, vp, C.c_float, C.POINTER(HairStruct), i32]
         _lib = l
     return _lib
 
@@ -145,6 +146,14 @@ def sdf_collide(grid, sdf_words: np.ndarray, margin: float, hair: OracleHair, th
                                                           C.byref(hair._struct), threads)
     if r:
         raise RuntimeError(f"oracle collide failed: {r}")
+
+
+def sdf_collide_mixed(grid, sdf_words: np.ndarray, margin: float, hair: OracleHair, threads: int = 0) -> None:
+    """CollideHairVerticesWithSdf (mixed forward / backward differences) on every vertex."""
+    gp = sdf_params(grid)
+    r = lib().tfxo_sdf_collide_mixed_f32(_p(sdf_words), C.addressof(gp), float(margin), C.byref(hair._struct), threads)
+    if r:
+        raise RuntimeError(f"oracle mixed collide failed: {r}")
 
 
 def mesh_skin(vertices: np.ndarray, skinning: np.ndarray, bones: np.ndarray, threads: int = 0) -> np.ndarray:

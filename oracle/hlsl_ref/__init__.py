@@ -55,6 +55,8 @@ def lib() -> C.CDLL:
         l.tfxr_sim_dispatch.argtypes = [C.c_int, vp, vp]
         l.tfxr_sdf_update.argtypes = [vp, C.c_int64, vp, vp, C.c_int, vp, C.c_int]
         l.tfxr_sdf_collide.argtypes = [vp, C.c_int64, vp, C.c_float, vp]
+        l.tfxr_sdf_collide_mixed.argtypes = [vp, C.c_int64, vp, C.c_float, vp]
+        l.tfxr_expand_strands.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int, vp]
         l.tfxr_mesh_skin.argtypes = [vp, vp, vp, vp, C.c_int]
         _lib = l
     return _lib

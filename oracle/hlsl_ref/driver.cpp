@@ -26,6 +26,7 @@
 #include "ref_sim.inc"
 #include "ref_sdf.inc"
 #include "ref_skin.inc"
+#include "ref_strands.inc"
 
 // ------------------------------------------------------------------------------------ fibers
 namespace {
@@ -202,6 +203,21 @@ extern "C" int tfxr_sdf_collide(uint32_t* sdf, int64_t allocCells, const SdfPara
     return 0;
 }
 
+// CollideHairVerticesWithSdf (the mixed-difference variant) over every vertex.
+extern "C" int tfxr_sdf_collide_mixed(uint32_t* sdf, int64_t allocCells, const SdfParamsF* g, float marginWorld,
+                                      const HairF* h) {
+    using namespace ref_sdf;
+    bind_sdf(g, sdf, allocCells);
+    const int64_t V = (int64_t)h->G * (h->F + 1) * h->n;
+    g_HairVertices.bind(h->pos, V);
+    g_PrevHairVertices.bind(h->prev, V);
+    g_CollisionMargin = marginWorld;
+    g_NumTotalHairVertices = (int)V;
+    g_NumHairVerticesPerStrand = h->n;
+    dispatch(CollideHairVerticesWithSdf, (int)std::ceil((float)V / (float)kGroup), false);
+    return 0;
+}
+
 // TressFXBoneSkinning::Update: BoneSkinning over every mesh vertex.
 extern "C" int tfxr_mesh_skin(float* out, const float* in, const float* skin, const float (*bones)[16], int nverts) {
     using namespace ref_skin;
@@ -211,5 +227,41 @@ extern "C" int tfxr_mesh_skin(float* out, const float* in, const float* skin, co
     g_NumMeshVertices[0] = nverts;
     load_bones(g_BoneSkinningMatrix, bones);
     dispatch(BoneSkinning, (int)std::ceil((float)nverts / (float)kGroup), false);
+    return 0;
+}
+
+// GetExpandedTressFXVert / GetExpandedTressFXShadowVert (TressFXStrands.hlsl) for every vertex id
+// [0, 2 * Vtot): out = {Position, Tangent, p0p1, StrandColor} per id (16 floats).  params = the
+// TressFXStrandParameters members in declaration order (MatBaseColor[4], MatTipColor[4], TipPercentage,
+// StrandUVTilingFactor, FiberRatio, FiberRadius as floats, then NumVerticesPerStrand, EnableThinTip
+// as ints); viewProj row-major, applied as mul(M, v).
+extern "C" int tfxr_expand_strands(const float* pos, const float* tan, int64_t vtot, const float* fparams,
+                                   const int* iparams, const float* eye, const float* win, const float* viewProj,
+                                   int shadow, float* out) {
+    using namespace ref_strands;
+    g_GuideHairVertexPositions.bind((void*)pos, vtot);
+    g_GuideHairVertexTangents.bind((void*)tan, vtot);
+    MatBaseColor = float4(fparams[0], fparams[1], fparams[2], fparams[3]);
+    MatTipColor = float4(fparams[4], fparams[5], fparams[6], fparams[7]);
+    TipPercentage = fparams[8];
+    StrandUVTilingFactor = fparams[9];
+    FiberRatio = fparams[10];
+    FiberRadius = fparams[11];
+    NumVerticesPerStrand = iparams[0];
+    EnableThinTip = iparams[1];
+    const int64_t strands = vtot / NumVerticesPerStrand;
+    std::vector<float2> texcd((size_t)strands);
+    g_HairStrandTexCd.bind(texcd.data(), strands);
+    float4x4 vp;
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) vp.m[r][c] = viewProj[4 * r + c];
+    const float3 e(eye[0], eye[1], eye[2]);
+    const float2 w(win[0], win[1]);
+    for (int64_t id = 0; id < 2 * vtot; ++id) {
+        TressFXVertex o = shadow ? GetExpandedTressFXShadowVert((uint)id, e, w, vp) : GetExpandedTressFXVert((uint)id, e, w, vp);
+        const float4 f[4] = {o.Position, o.Tangent, o.p0p1, o.StrandColor};
+        for (int k = 0; k < 4; ++k)
+            for (int c = 0; c < 4; ++c) out[16 * id + 4 * k + c] = f[k][c];
+    }
     return 0;
 }

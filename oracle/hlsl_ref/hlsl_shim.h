@@ -31,13 +31,27 @@ struct SwzXYZ {
     inline SwzXYZ& operator*=(float s);
 };
 
+// A two-component view (.xy) over the first two floats of a float2 or float4.
+template <int N>
+struct SwzXY {
+    float e[N];
+    inline operator struct float2() const;
+};
+
 struct float2 {
-    float x, y;
+    union {
+        struct { float x, y; };
+        SwzXY<2> xy;
+    };
     float2() : x(0), y(0) {}
     float2(float a, float b) : x(a), y(b) {}
+    float2(const float2& o) : x(o.x), y(o.y) {}
+    template <int N> float2(const SwzXY<N>& s) : x(s.e[0]), y(s.e[1]) {}
+    float2& operator=(const float2& o) { x = o.x; y = o.y; return *this; }
     float& operator[](int i) { return (&x)[i]; }
     float operator[](int i) const { return (&x)[i]; }
 };
+template <int N> inline SwzXY<N>::operator float2() const { return float2(e[0], e[1]); }
 
 struct float3 {
     union {
@@ -58,10 +72,13 @@ struct float4 {
     union {
         struct { float x, y, z, w; };
         SwzXYZ<4> xyz;
+        SwzXY<4> xy;
     };
     float4() : x(0), y(0), z(0), w(0) {}
     float4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
     float4(const float3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    float4(const float2& v, float c, float d) : x(v.x), y(v.y), z(c), w(d) {}
+    float4(const float2& a, const float2& b) : x(a.x), y(a.y), z(b.x), w(b.y) {}
     float4(const float4& o) : x(o.x), y(o.y), z(o.z), w(o.w) {}
     float4& operator=(const float4& o) { x = o.x; y = o.y; z = o.z; w = o.w; return *this; }
     float& operator[](int i) { return (&x)[i]; }
@@ -106,6 +123,10 @@ struct int3 {
 inline int3 operator-(const int3& a, const int3& b) { return int3(a.x - b.x, a.y - b.y, a.z - b.z); }
 inline int3 operator+(const int3& a, const int3& b) { return int3(a.x + b.x, a.y + b.y, a.z + b.z); }
 
+struct int2 {
+    int x, y;
+};
+
 struct uint3 {
     uint x, y, z;
     uint3() : x(0), y(0), z(0) {}
@@ -142,6 +163,12 @@ inline float4x4 operator*(const float4x4& a, float s) {
     for (int r = 0; r < 4; ++r) for (int c = 0; c < 4; ++c) o.m[r][c] = a.m[r][c] * s;
     return o;
 }
+// mul(M, v) (column vector): r[i] = ((M[i][0]*v.x + M[i][1]*v.y) + M[i][2]*v.z) + M[i][3]*v.w
+inline float4 mul(const float4x4& M, const float4& v) {
+    float o[4];
+    for (int r = 0; r < 4; ++r) o[r] = ((M.m[r][0] * v.x + M.m[r][1] * v.y) + M.m[r][2] * v.z) + M.m[r][3] * v.w;
+    return float4(o[0], o[1], o[2], o[3]);
+}
 inline float4 mul(const float4& v, const float4x4& M) {
     float o[4];
     for (int c = 0; c < 4; ++c) o[c] = ((v.x * M.m[0][c] + v.y * M.m[1][c]) + v.z * M.m[2][c]) + v.w * M.m[3][c];
@@ -149,6 +176,20 @@ inline float4 mul(const float4& v, const float4x4& M) {
 }
 
 // ------------------------------------------------------------------------------------ intrinsics
+inline float2 operator*(const float2& a, float s) { return float2(a.x * s, a.y * s); }
+inline float2 operator/(const float2& a, float s) { return float2(a.x / s, a.y / s); }
+inline float length(const float2& a) { return std::sqrt(a.x * a.x + a.y * a.y); }
+inline float3& operator*=(float3& a, const float3& b) { a = a * b; return a; }
+inline float4 operator*(const float4& a, const float4& b) { return float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+// rcp: the IEEE reciprocal; lerp(x, y, s) = x + s * (y - x)
+inline float rcp(float a) { return 1.0f / a; }
+inline float lerp(float x, float y, float s) { return x + s * (y - x); }
+inline float3 lerp(const float3& x, const float3& y, float s) { return x + (y - x) * s; }
+struct SamplerState {};
+// Texture sampling is a graphics operation; here every texture is white.
+template <class T> struct Texture2D {
+    T SampleLevel(const SamplerState&, const float2&, float) const { return T(1.0f, 1.0f, 1.0f, 1.0f); }
+};
 inline float dot(const float3& a, const float3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline float3 cross(const float3& a, const float3& b) {
     return float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);

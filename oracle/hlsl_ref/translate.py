@@ -14,7 +14,11 @@ The rewrites, in order:
      index them with a float bone index);
   7. the scalar swizzle `sharedLength[i].x` on a float array reads `sharedLength[i]`;
   8. for TressFXBoneSkinning.hlsl only the compute part (up to the "// visualization" comment) is
-     kept; the vertex/pixel shaders after it are rendering code.
+     kept; the vertex/pixel shaders after it are rendering code;
+  9. the strand expansion unit (ref_strands) is TressFXStrands.hlsl without its #include, preceded
+     by what it uses from the other files: the TRESSFX_FLOAT_EPSILON define, MatrixMult and the two
+     Safe_normalize overloads of TressFXUtilities.hlsl, and the cbuffer TressFXStrandParameters of
+     TressFXRendering.hlsl; `.rgb` reads `.xyz` and `(TressFXVertex)0` value-initialises.
 
 The output is wrapped in a namespace per shader file and compiled against hlsl_shim.h.
 """
@@ -29,7 +33,37 @@ SHADERS = {
     "ref_sim": "src/Shaders/TressFXSimulation.hlsl",
     "ref_sdf": "src/Shaders/TressFXSDFCollision.hlsl",
     "ref_skin": "src/Shaders/TressFXBoneSkinning.hlsl",
+    "ref_strands": "src/Shaders/TressFXStrands.hlsl",
 }
+
+
+def _function(text: str, signature_re: str) -> str:
+    """The full text (signature + body) of the first function whose signature matches."""
+    m = re.search(signature_re, text)
+    if not m:
+        raise ValueError(f"function {signature_re} not found")
+    j = text.index("{", m.end())
+    depth, k = 1, j + 1
+    while depth:
+        depth += {"{": 1, "}": -1}.get(text[k], 0)
+        k += 1
+    return text[m.start():k]
+
+
+def _strands_unit() -> str:
+    util = (REF / "src/Shaders/TressFXUtilities.hlsl").read_text()
+    rend = (REF / "src/Shaders/TressFXRendering.hlsl").read_text()
+    strands = (REF / "src/Shaders/TressFXStrands.hlsl").read_text()
+    eps = re.search(r"#define\s+TRESSFX_FLOAT_EPSILON[^\n]*", util).group(0)
+    m = re.search(r"\[\[vk::binding[^\n]*\]\]\s*cbuffer\s+TressFXStrandParameters[^{]*\{", rend)
+    cb = _function(rend[m.start():], r"cbuffer\s+TressFXStrandParameters")
+    parts = [eps, cb, _function(util, r"float4\s+MatrixMult\s*\("),
+             _function(util, r"float2\s+Safe_normalize\s*\(\s*float2"),
+             _function(util, r"float3\s+Safe_normalize\s*\(\s*float3"),
+             re.sub(r'#include\s+"[^"]+"', "", strands)]
+    s = "\n\n".join(parts)
+    s = s.replace(".rgb", ".xyz").replace("(TressFXVertex)0", "TressFXVertex()")
+    return s
 
 
 def _unwrap_cbuffers(s: str) -> str:
@@ -84,7 +118,8 @@ def main(out_dir: Path) -> list[Path]:
         if not src.exists():
             raise FileNotFoundError(src)
         dst = out_dir / f"{name}.inc"
-        dst.write_text(translate(src.read_text(), name))
+        text = _strands_unit() if name == "ref_strands" else src.read_text()
+        dst.write_text(translate(text, name))
         written.append(dst)
     return written
 

@@ -607,6 +607,45 @@ template <class T> static void sdf_collide_vertex(const typename SdfWord<T>::typ
     }
 }
 
+// CollideHairVerticesWithSdf, TressFXSDFCollision.hlsl:599-715 (one vertex; every vertex of the
+// object, roots included): one 8-corner fetch, the gradient by forward or backward differences inside
+// the same cell, with h = 0.1 * cellSize added to the cell-normalised coordinates as the shader does.
+template <class T> static void sdf_collide_mixed_vertex(const typename SdfWord<T>::type* sdf, const Grid<T>& g, T margin,
+                                                        T* pos, T* prev, int64_t v) {
+    V4<T> hv = ld4(pos, v);
+    V3<T> p = xyz(hv);
+    int gc[3];
+    sdf_coords(g, p, gc);
+    if (!(0 <= gc[0] && gc[0] < g.nx - 2) || !(0 <= gc[1] && gc[1] < g.ny - 2) || !(0 <= gc[2] && gc[2] < g.nz - 2)) return;
+    int64_t base = (int64_t)g.nx * g.ny * gc[2] + (int64_t)g.nx * gc[1] + gc[0];
+    int64_t X = 1, Y = g.nx, Z = (int64_t)g.ny * g.nx;
+    const int64_t off[8] = {0, X, Y, Y + X, Z, Z + X, Z + Y, Z + Y + X};
+    T d[8];
+    for (int j = 0; j < 8; ++j) {
+        d[j] = as_dist<T>(sdf, base + off[j]);
+        if (d[j] == T(1e10f)) return;
+    }
+    auto tri = [&](T x, T y, T z) {
+        T b0 = lerp(lerp(d[0], d[1], x), lerp(d[2], d[3], x), y);
+        T b1 = lerp(lerp(d[4], d[5], x), lerp(d[6], d[7], x), y);
+        return lerp(b0, b1, z);
+    };
+    V3<T> cp = sdf_cell_pos(g, gc[0], gc[1], gc[2]);
+    V3<T> ip = (p - cp) / g.cell;
+    T dist = tri(ip.x, ip.y, ip.z);
+    T h = T(0.1f) * g.cell;
+    V3<T> dir = {(ip.x + h < T(1.0f)) ? T(1.0f) : T(-1.0f), (ip.y + h < T(1.0f)) ? T(1.0f) : T(-1.0f),
+                 (ip.z + h < T(1.0f)) ? T(1.0f) : T(-1.0f)};
+    V3<T> nd = {tri(ip.x + h * dir.x, ip.y, ip.z), tri(ip.x, ip.y + h * dir.y, ip.z), tri(ip.x, ip.y, ip.z + h * dir.z)};
+    V3<T> grad = {(dir.x * (nd.x - dist)) / h, (dir.y * (nd.y - dist)) / h, (dir.z * (nd.z - dist)) / h};
+    V3<T> nrm = normalize(grad);
+    if (dist < margin) {
+        V3<T> proj = p + nrm * (margin - dist);
+        st3(pos, v, proj);
+        st3(prev, v, proj);
+    }
+}
+
 // BoneSkinning, src/Shaders/TressFXBoneSkinning.hlsl:57-94 (collision-mesh LBS; one vertex)
 static void mesh_skin_vertex(float* out, const float* in, const float* skin, const float* bones, int64_t v) {
     const float* pin = in + 8 * v;
@@ -742,6 +781,23 @@ extern "C" int tfxo_sdf_collide_f64(const void* sdf, const void* gp, float margi
     return run_collide<double>(sdf, (const SdfParamsF*)gp, margin, h, threads);
 }
 
+template <class T> static int run_collide_mixed(const void* sdfv, const SdfParamsF* gp, float margin, const tfxo_hair* hd,
+                                                int threads) {
+    using W = typename SdfWord<T>::type;
+    if (!sdfv || !gp || !hd) return 1;
+    Hair<T> h = view<T>(hd);
+    Grid<T> g = load_grid<T>(gp);
+    int64_t vtot = (int64_t)h.G * (h.F + 1) * h.n;
+    const W* sdf = (const W*)sdfv;
+    parallel_for(vtot, threads, [&](int64_t b, int64_t e) {
+        for (int64_t v = b; v < e; ++v) sdf_collide_mixed_vertex<T>(sdf, g, T(margin), h.pos, h.prev, v);
+    });
+    return 0;
+}
+extern "C" int tfxo_sdf_collide_mixed_f32(const void* sdf, const void* gp, float margin, const tfxo_hair* h, int threads) {
+    return run_collide_mixed<float>(sdf, (const SdfParamsF*)gp, margin, h, threads);
+}
+
 // Collision-mesh bone skinning (BoneSkinning kernel, one thread per mesh vertex).
 // in/out: {float4 position, float4 normal}[Vm] (w copied from in); skin: {float4 idx, float4 w}[Vm].
 extern "C" int tfxo_mesh_skin_f32(float* out, const float* in, const float* skin, const float* bones, int64_t nverts, int threads) {
@@ -756,3 +812,77 @@ extern "C" int tfxo_mesh_skin_f32(float* out, const float* in, const float* skin
     return 0;
 }
 
+// ================================================================================================
+// Strand quad expansion: GetExpandedTressFXVert / GetExpandedTressFXShadowVert
+// (src/Shaders/TressFXStrands.hlsl), the vertex-shader arithmetic that turns each hair vertex into
+// two camera-facing quad vertices.  Conventions: Safe_normalize (TressFXUtilities.hlsl:104-119) with
+// rcp = the IEEE reciprocal; lerp(x, y, s) = x + s (y - x); mul(M, v) summed left to right over the
+// row; the albedo texture is white (texture sampling is graphics).
+namespace {
+struct F2 { float x, y; };
+struct F3x { float x, y, z; };
+inline F3x sub3(F3x a, F3x b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline F3x scl3(F3x a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline F3x add3(F3x a, F3x b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline F3x safe3(F3x v) {
+    const float len = std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+    if (!(len >= 1e-7f)) return {0.0f, 0.0f, 0.0f};
+    return scl3(v, 1.0f / len);
+}
+inline F2 safe2(F2 v) {
+    const float len = std::sqrt(v.x * v.x + v.y * v.y);
+    if (!(len >= 1e-7f)) return {0.0f, 0.0f};
+    const float r = 1.0f / len;
+    return {v.x * r, v.y * r};
+}
+inline void mulMv(const float* M, const float v[4], float o[4]) {
+    for (int r = 0; r < 4; ++r) o[r] = ((M[4 * r] * v[0] + M[4 * r + 1] * v[1]) + M[4 * r + 2] * v[2]) + M[4 * r + 3] * v[3];
+}
+}  // namespace
+
+extern "C" int tfxo_expand_strands(const float* pos, const float* tan, int64_t vtot, const float* fp, const int* ip,
+                                   const float* eye, const float* win, const float* VP, int shadow, float* out) {
+    if (!pos || !tan || !fp || !ip || !eye || !win || !VP || !out || ip[0] < 2) return 1;
+    const int n = ip[0], thinTip = ip[1];
+    const F3x eyeV = {eye[0], eye[1], eye[2]};
+    for (int64_t id = 0; id < 2 * vtot; ++id) {
+        const uint32_t vid = (uint32_t)id;
+        const int64_t index = vid / 2;
+        const F3x v = {pos[4 * index], pos[4 * index + 1], pos[4 * index + 2]};
+        const F3x t = {tan[4 * index], tan[4 * index + 1], tan[4 * index + 2]};
+        const uint32_t inStrand = (uint32_t)(index % n);
+        const float fraction = (float)inStrand / (float)(n - 1);
+        const float ratio = thinTip > 0 ? 1.0f + fraction * (fp[10] - 1.0f) : 1.0f;
+        const F3x vv = safe3(sub3(v, eyeV));
+        const F3x right = safe3({t.y * vv.z - t.z * vv.y, t.z * vv.x - t.x * vv.z, t.x * vv.y - t.y * vv.x});
+        const float r4[4] = {right.x, right.y, right.z, 0.0f};
+        float pr[4];
+        mulMv(VP, r4, pr);
+        const F2 projRight = safe2({pr[0], pr[1]});
+        const float expandPixels = shadow ? 1.0f : 0.71f;
+        const F3x p0 = add3(v, scl3(scl3(scl3(right, -1.0f), ratio), fp[11]));
+        const F3x p1 = add3(v, scl3(scl3(scl3(right, 1.0f), ratio), fp[11]));
+        const float h0[4] = {p0.x, p0.y, p0.z, 1.0f}, h1[4] = {p1.x, p1.y, p1.z, 1.0f};
+        float e0[4], e1[4];
+        mulMv(VP, h0, e0);
+        mulMv(VP, h1, e1);
+        const bool odd = (vid & 1u) != 0;
+        const float fDir = odd ? -1.0f : 1.0f;
+        const float* sel = odd ? e0 : e1;
+        const float offv[4] = {(projRight.x * expandPixels) / win[1], (projRight.y * expandPixels) / win[1], 0.0f, 0.0f};
+        float* o = out + 16 * id;
+        for (int c = 0; c < 4; ++c) o[c] = sel[c] + (fDir * offv[c]) * sel[3];
+        for (int c = 4; c < 16; ++c) o[c] = 0.0f;
+        if (shadow) continue;
+        const float uvx = odd ? 0.0f : 1.0f;
+        o[4] = t.x; o[5] = t.y; o[6] = t.z; o[7] = uvx;
+        const float w0 = std::fmax(e0[3], 1e-7f), w1 = std::fmax(e1[3], 1e-7f);
+        o[8] = e0[0] / w0; o[9] = e0[1] / w0; o[10] = e1[0] / w1; o[11] = e1[1] / w1;
+        const F3x root = {1.0f * fp[0], 1.0f * fp[1], 1.0f * fp[2]};
+        const F3x tip = {fp[4], fp[5], fp[6]};
+        const float rootRange = 1.0f - fp[8];
+        const F3x col = fraction > rootRange ? add3(root, scl3(sub3(tip, root), fraction)) : root;
+        o[12] = col.x; o[13] = col.y; o[14] = col.z; o[15] = fraction;
+    }
+    return 0;
+}

@@ -93,6 +93,15 @@ class HairDesc(C.Structure):
                 ("follow_hairs_per_guide", C.c_int32), ("reserved", C.c_int32)]
 
 
+class StrandParams(C.Structure):
+    """TressFXStrandParams (cbuffer TressFXStrandParameters, TressFXRendering.hlsl:61-80)."""
+    _fields_ = [("mat_base_color", C.c_float * 4), ("mat_tip_color", C.c_float * 4), ("tip_percentage", C.c_float),
+                ("strand_uv_tiling_factor", C.c_float), ("fiber_ratio", C.c_float), ("fiber_radius", C.c_float),
+                ("num_vertices_per_strand", C.c_int32), ("enable_thin_tip", C.c_int32), ("node_pool_size", C.c_int32),
+                ("render_params_index", C.c_int32), ("enable_strand_uv", C.c_int32),
+                ("enable_strand_tangent", C.c_int32), ("padding", C.c_int32 * 2)]
+
+
 class SdfGrid(C.Structure):
     """Grid part of TressFXSDFCollisionParams (TressFXConstantBuffers.h:119-134)."""
     _fields_ = [("origin", C.c_float * 4), ("cell_size", C.c_float),
@@ -155,6 +164,7 @@ _PROTOS = {
     "tfx_hair_write_async": (C.c_int, [P, C.c_int, P, C.c_size_t]),
     "tfx_hair_get_buffer": (C.c_int, [P, C.c_int, C.POINTER(P), C.POINTER(C.c_size_t)]),
     "tfx_hair_get_counts": (C.c_int, [P, C.POINTER(C.c_int32)]),
+    "tfx_hair_expand_strands": (C.c_int, [P, C.POINTER(StrandParams), FP, FP, FP, C.c_int, P]),
     "tfx_sdf_grid_from_bbox": (C.c_int, [FP, FP, C.c_int, C.POINTER(SdfGrid), FP, C.POINTER(C.c_int64)]),
     "tfx_sdf_grid_origin": (C.c_int, [FP, F32, C.POINTER(SdfGrid)]),
     "tfx_sdf_create": (C.c_int, [P, C.c_int64, C.POINTER(P)]),
@@ -163,6 +173,7 @@ _PROTOS = {
     "tfx_sdf_update": (C.c_int, [P, C.POINTER(SdfGrid)]),
     "tfx_sdf_dispatch": (C.c_int, [P, C.c_int, C.POINTER(SdfGrid)]),
     "tfx_sdf_collide": (C.c_int, [P, P, C.POINTER(SdfGrid), F32]),
+    "tfx_sdf_collide_mixed": (C.c_int, [P, P, C.POINTER(SdfGrid), F32]),
     "tfx_sdf_read": (C.c_int, [P, P, C.c_size_t]),
     "tfx_sdf_write": (C.c_int, [P, P, C.c_size_t]),
     "tfx_sdf_get_buffer": (C.c_int, [P, C.POINTER(P), C.POINTER(C.c_size_t)]),

@@ -291,6 +291,11 @@ class SDFCollision:
     def collide(self, hair: HairObject, grid: A.SdfGrid, margin_world: float) -> None:
         check(A.lib().tfx_sdf_collide(self.handle, hair.handle, C.byref(grid), float(margin_world)), "tfx_sdf_collide")
 
+    def collide_mixed(self, hair: HairObject, grid: A.SdfGrid, margin_world: float) -> None:
+        """CollideHairVerticesWithSdf, the mixed forward / backward difference variant."""
+        check(A.lib().tfx_sdf_collide_mixed(self.handle, hair.handle, C.byref(grid), float(margin_world)),
+              "tfx_sdf_collide_mixed")
+
     def read(self, cells: int) -> np.ndarray:
         out = np.empty(cells, dtype=np.uint32)
         check(A.lib().tfx_sdf_read(self.handle, ptr(out), out.nbytes), "tfx_sdf_read")

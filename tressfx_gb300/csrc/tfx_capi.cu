@@ -403,6 +403,25 @@ extern "C" int tfx_hair_get_counts(tfx_hair h, int32_t out[4]) {
     return TFX_OK;
 }
 
+// ============================================================================ strand quads
+extern "C" int tfx_hair_expand_strands(tfx_hair h, const tfx_strand_params* p, const float eye[3], const float win[2],
+                                       const float vp[16], int shadow, void* out) {
+    if (!h || !p || !eye || !win || !vp || !out) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_hair_expand_strands: null argument");
+    if (p->num_vertices_per_strand != h->n)
+        return fail(TFX_ERR_MISMATCH, "tfx_hair_expand_strands: %d vertices per strand, object has %d", p->num_vertices_per_strand, h->n);
+    if (((uintptr_t)out & 15) != 0) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_hair_expand_strands: output not 16-byte aligned");
+    ExpandParams P{};
+    for (int k = 0; k < 4; ++k) { P.baseColor[k] = p->mat_base_color[k]; P.tipColor[k] = p->mat_tip_color[k]; }
+    P.tipPercentage = p->tip_percentage; P.fiberRatio = p->fiber_ratio; P.fiberRadius = p->fiber_radius;
+    P.n = h->n; P.enableThinTip = p->enable_thin_tip; P.shadow = shadow ? 1 : 0;
+    for (int k = 0; k < 3; ++k) P.eye[k] = eye[k];
+    P.winH = win[1];
+    for (int k = 0; k < 16; ++k) P.viewProj[k] = vp[k];
+    TFX_CUDA(cudaSetDevice(h->ctx->device), "cudaSetDevice");
+    cudaError_t e = launch_expand_strands(h->view.pos, h->view.tan, h->Vtot, P, static_cast<float4*>(out), h->ctx->stream);
+    return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_hair_expand_strands launch");
+}
+
 // ============================================================================ SDF
 extern "C" int tfx_sdf_create(tfx_context ctx, int64_t alloc_cells, tfx_sdf* out) {
     if (!out) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_sdf_create: out is null");
@@ -494,6 +513,15 @@ extern "C" int tfx_sdf_collide(tfx_sdf s, tfx_hair h, const tfx_sdf_grid* grid, 
     return TFX_OK;
 }
 
+extern "C" int tfx_sdf_collide_mixed(tfx_sdf s, tfx_hair h, const tfx_sdf_grid* grid, float margin_world) {
+    SdfGrid g;
+    if (int r = check_grid(s, grid, &g, "tfx_sdf_collide_mixed")) return r;
+    if (!h) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_sdf_collide_mixed: null hair");
+    TFX_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaError_t e = launch_sdf_collide_mixed(s->grid, g, margin_world, h->view.pos, h->view.prev, h->Vtot, s->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "SDF mixed collide launch");
+    return TFX_OK;
+}
 extern "C" int tfx_sdf_read(tfx_sdf s, void* dst, size_t bytes) {
     if (!s || (!dst && bytes)) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_sdf_read: bad argument");
     if (bytes > 4 * (size_t)s->alloc) return fail(TFX_ERR_SIZE, "tfx_sdf_read: %zu bytes > allocation", bytes);

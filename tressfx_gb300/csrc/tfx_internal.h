@@ -57,6 +57,19 @@ cudaError_t launch_sdf_construct(uint32_t* sdf, const SdfGrid& g, const float4* 
 cudaError_t launch_sdf_finalize(uint32_t* sdf, int64_t cells, cudaStream_t s);
 cudaError_t launch_sdf_collide(const uint32_t* sdf, const SdfGrid& g, float margin, float4* pos, float4* prev,
                                int n, int64_t vtot, cudaStream_t s);
+// Strand quad expansion (TressFXStrands.hlsl GetExpandedTressFXVert), by value into the kernel.
+struct ExpandParams {
+    float baseColor[4], tipColor[4];
+    float tipPercentage, fiberRatio, fiberRadius;
+    int n, enableThinTip, shadow;
+    float eye[3];
+    float winH;
+    float viewProj[16];   // row-major, applied as mul(M, v)
+};
+cudaError_t launch_expand_strands(const float4* pos, const float4* tan, int64_t vtot, const ExpandParams& P, float4* out,
+                                  cudaStream_t s);
+cudaError_t launch_sdf_collide_mixed(const uint32_t* sdf, const SdfGrid& g, float margin, float4* pos, float4* prev,
+                                     int64_t vtot, cudaStream_t s);
 cudaError_t launch_mesh_skin(float4* out, const float4* in, const float4* skin, const float4* bones, int nverts,
                              cudaStream_t s);
 

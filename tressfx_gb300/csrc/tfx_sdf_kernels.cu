@@ -85,6 +85,48 @@ __global__ void __launch_bounds__(256) k_sdf_collide(const float* __restrict__ s
 
 // BoneSkinning, src/Shaders/TressFXBoneSkinning.hlsl:57-94.  One thread per mesh vertex.
 // in/out: {float4 position, float4 normal}; skin: {float4 boneIndex, float4 boneWeight}.
+// CollideHairVerticesWithSdf (TressFXSDFCollision.hlsl:599-715), the mixed-difference variant: one
+// thread per vertex (roots included), one 8-corner fetch, the gradient by forward or backward
+// differences within the same cell (h = 0.1 * cellSize added to the cell-normalised coordinates,
+// as the shader writes it).
+__global__ void __launch_bounds__(256) k_sdf_collide_mixed(const float* __restrict__ sdf, SdfGrid g, float margin,
+                                                           float4* __restrict__ pos, float4* __restrict__ prev,
+                                                           int64_t vtot) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= vtot) return;
+    const float4 hv = pos[v];
+    const float3 p = xyz(hv);
+    const int3 gc = sdf_coords(g, p);
+    if (!(0 <= gc.x && gc.x < g.nx - 2) || !(0 <= gc.y && gc.y < g.ny - 2) || !(0 <= gc.z && gc.z < g.nz - 2)) return;
+    const long long X = 1, Y = g.nx, Z = (long long)g.ny * g.nx;
+    const long long base = Z * gc.z + Y * gc.y + gc.x;
+    const long long off[8] = {0, X, Y, Y + X, Z, Z + X, Z + Y, Z + Y + X};
+    float d[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        d[j] = __ldg(sdf + base + off[j]);
+        if (d[j] == 1e10f) return;
+    }
+    auto tri = [&](float x, float y, float z) {
+        const float b0 = lerp_ref(lerp_ref(d[0], d[1], x), lerp_ref(d[2], d[3], x), y);
+        const float b1 = lerp_ref(lerp_ref(d[4], d[5], x), lerp_ref(d[6], d[7], x), y);
+        return lerp_ref(b0, b1, z);
+    };
+    const float3 cp = sdf_cell_pos(g, gc.x, gc.y, gc.z);
+    const float3 ip = divs(sub(p, cp), g.cell);
+    const float dist = tri(ip.x, ip.y, ip.z);
+    const float h = 0.1f * g.cell;
+    const float3 dir = mk3((ip.x + h < 1.0f) ? 1.0f : -1.0f, (ip.y + h < 1.0f) ? 1.0f : -1.0f, (ip.z + h < 1.0f) ? 1.0f : -1.0f);
+    const float3 nd = mk3(tri(ip.x + h * dir.x, ip.y, ip.z), tri(ip.x, ip.y + h * dir.y, ip.z), tri(ip.x, ip.y, ip.z + h * dir.z));
+    const float3 grad = mk3((dir.x * (nd.x - dist)) / h, (dir.y * (nd.y - dist)) / h, (dir.z * (nd.z - dist)) / h);
+    const float3 nrm = normalize(grad);
+    if (dist < margin) {
+        const float3 proj = add(p, mul(nrm, margin - dist));
+        pos[v] = with_xyz(hv, proj);
+        prev[v] = with_xyz(prev[v], proj);
+    }
+}
+
 __global__ void __launch_bounds__(256) k_mesh_skin(float4* __restrict__ out, const float4* __restrict__ in,
                                                    const float4* __restrict__ skin, const float4* __restrict__ bones,
                                                    int nverts) {
@@ -128,6 +170,14 @@ cudaError_t launch_sdf_collide(const uint32_t* sdf, const SdfGrid& g, float marg
     if (vtot <= 0) return cudaSuccess;
     k_sdf_collide<<<(unsigned)((vtot + 255) / 256), 256, 0, s>>>(reinterpret_cast<const float*>(sdf), g, margin, pos,
                                                                  prev, n, vtot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sdf_collide_mixed(const uint32_t* sdf, const SdfGrid& g, float margin, float4* pos, float4* prev,
+                                     int64_t vtot, cudaStream_t s) {
+    if (vtot <= 0) return cudaSuccess;
+    k_sdf_collide_mixed<<<(unsigned)((vtot + 255) / 256), 256, 0, s>>>(reinterpret_cast<const float*>(sdf), g, margin, pos,
+                                                                       prev, vtot);
     return cudaGetLastError();
 }
 
