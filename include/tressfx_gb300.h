@@ -276,6 +276,40 @@ int tfx_sdf_get_buffer(tfx_sdf sdf, void** device_ptr, size_t* bytes);
 int tfx_sdf_build_static(tfx_context ctx, const tfx_sdf_grid* grid, const void* mesh_vertices, int num_vertices,
                          const uint32_t* indices, int num_triangles, float* sdf_out);
 
+/* ---------------------------------------------------------------------------------- SDF marching cubes */
+/* TressFXSDFMarchingCubes (src/TressFX/TressFXSDFMarchingCubes.{h,cpp}): the iso-surface of a signed
+ * distance grid as a triangle soup in a device buffer of {float4 position, float4 normal}
+ * [max_vertices] (StandardVertex of TressFXMarchingCubes.hlsl:33-37), headless. */
+typedef struct tfx_mc_t* tfx_mc;
+/* Constructor + Initialize (TressFXSDFMarchingCubes.cpp:27-118): the vertex buffer (128*1024 vertices
+ * in the reference), the counter, and scratch for grids of up to max_cells cells (< 2^31 - 4096).  The
+ * tables start as tfx_mc_default_tables'; the iso level starts at 0. */
+int tfx_mc_create(tfx_context ctx, int max_vertices, int64_t max_cells, tfx_mc* out);
+int tfx_mc_destroy(tfx_mc mc);
+/* The library's own tables in the layout of MARCHING_CUBES_EDGE_TABLE[256] and
+ * MARCHING_CUBES_TRIANGLE_TABLE[256*16] (src/MarchingCubesTables.h): a bit per crossing edge, and up
+ * to five triangles of edge indices per configuration, -1 terminated.  Built from the cube's faces,
+ * they separate the inside corners on every ambiguous face the same way in both cubes that share it,
+ * so the surface is closed across cubes.  Host-only. */
+int tfx_mc_default_tables(int32_t* edge_table, int32_t* tri_table);
+/* Uploads the two tables the kernel reads (the reference's Initialize uploads its own,
+ * TressFXSDFMarchingCubes.cpp:95-99); passing the reference's reproduces its triangles exactly.
+ * Both null restores the defaults.  Triangle entries must be -1 or an edge 0..11. */
+int tfx_mc_set_tables(tfx_mc mc, const int32_t* edge_table, const int32_t* tri_table);
+/* SetSDFIsoLevel (TressFXSDFMarchingCubes.h:69), in cells: the surface is value = cell_size * iso. */
+int tfx_mc_set_iso_level(tfx_mc mc, float iso_level);
+/* Update (TressFXSDFMarchingCubes.cpp:168-232): InitializeMCVertices + RunMarchingCubesOnSdf over the
+ * finalized grid of `sdf`.  The vertex order is cell-index order (the reference's atomic append
+ * order is unspecified); a cube is written only if its vertices end below max_vertices, and the
+ * counter holds the vertices every cube reserved, as the shader's counter does.  Vertices not
+ * written are zero.  Stream-ordered; nothing synchronizes. */
+int tfx_mc_update(tfx_mc mc, tfx_sdf sdf, const tfx_sdf_grid* grid);
+/* The same over any DEVICE float grid [X*Y*Z] (a batch SDF, tfx_sdf_build_static's output). */
+int tfx_mc_run(tfx_mc mc, const float* sdf_device, const tfx_sdf_grid* grid);
+int tfx_mc_get_buffers(tfx_mc mc, void** vertices, int32_t** num_vertices);
+/* Copies `bytes` of the vertex buffer and the counter to the host (synchronizes the stream). */
+int tfx_mc_read(tfx_mc mc, void* host_vertices, size_t bytes, int32_t* num_vertices);
+
 /* ---------------------------------------------------------------------------------- collision mesh */
 /* TressFXBoneSkinning::Initialize (TressFXBoneSkinning.cpp:287-404): uploads the bind-pose mesh
  * {float4 position, float4 normal}[num_vertices], uint32[3*num_triangles] and per-vertex

@@ -54,6 +54,7 @@ def lib() -> C.CDLL:
         l.tfxo_ifloat_flip3.restype = C.c_uint32
         l.tfxo_mesh_skin_f32.argtypes = [vp, vp, vp, vp, i64, i32]
         l.tfxo_sdf_collide_mixed_f32.argtypes = [vp, vp, C.c_float, C.POINTER(HairStruct), i32]
+        l.tfxo_marching_cubes_f32.argtypes = [vp, vp, C.c_float, vp, vp, i32, vp, vp]
         _lib = l
     return _lib
 
@@ -154,6 +155,24 @@ def sdf_collide_mixed(grid, sdf_words: np.ndarray, margin: float, hair: OracleHa
     r = lib().tfxo_sdf_collide_mixed_f32(_p(sdf_words), C.addressof(gp), float(margin), C.byref(hair._struct), threads)
     if r:
         raise RuntimeError(f"oracle mixed collide failed: {r}")
+
+
+def marching_cubes(grid, sdf: np.ndarray, iso: float, edge_table: np.ndarray, tri_table: np.ndarray,
+                   max_vertices: int) -> tuple[np.ndarray, int]:
+    """RunMarchingCubesOnSdf in cell-index order: ({position, normal}[max_vertices] as (max, 8) float32,
+    the counter).  `iso` is the world-unit iso value (cell size * iso level)."""
+    gp = sdf_params(grid)
+    f = np.ascontiguousarray(np.asarray(sdf).view(np.float32) if np.asarray(sdf).dtype == np.uint32 else sdf,
+                             dtype=np.float32)
+    e = np.ascontiguousarray(edge_table, dtype=np.int32)
+    t = np.ascontiguousarray(tri_table, dtype=np.int32).reshape(-1)
+    out = np.zeros((max_vertices, 8), np.float32)
+    cnt = np.zeros(1, np.int32)
+    r = lib().tfxo_marching_cubes_f32(_p(f), C.addressof(gp), float(np.float32(iso)), _p(e), _p(t), int(max_vertices),
+                                      _p(out), _p(cnt))
+    if r:
+        raise RuntimeError(f"oracle marching cubes failed: {r}")
+    return out, int(cnt[0])
 
 
 def mesh_skin(vertices: np.ndarray, skinning: np.ndarray, bones: np.ndarray, threads: int = 0) -> np.ndarray:

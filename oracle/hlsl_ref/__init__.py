@@ -37,7 +37,8 @@ def build(force: bool = False) -> Path:
     translate.main(REF_DIR)
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math",
-           "-fno-strict-aliasing", "-fPIC", "-shared", "-w", f"-I{HERE}", f"-I{REF_DIR}", "-o", str(tmp),
+           "-fno-strict-aliasing", "-fPIC", "-shared", "-w", f"-I{HERE}", f"-I{REF_DIR}",
+           f"-I{SHADER_ROOT / 'src'}", "-o", str(tmp),
            str(HERE / "driver.cpp")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -58,6 +59,8 @@ def lib() -> C.CDLL:
         l.tfxr_sdf_collide_mixed.argtypes = [vp, C.c_int64, vp, C.c_float, vp]
         l.tfxr_expand_strands.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp, vp, C.c_int, vp]
         l.tfxr_mesh_skin.argtypes = [vp, vp, vp, vp, C.c_int]
+        l.tfxr_mc_tables.argtypes = [vp, vp]
+        l.tfxr_marching_cubes.argtypes = [vp, C.c_int64, vp, C.c_float, vp, vp, C.c_int, vp, vp]
         _lib = l
     return _lib
 

@@ -27,6 +27,9 @@
 #include "ref_sdf.inc"
 #include "ref_skin.inc"
 #include "ref_strands.inc"
+#include "ref_mc.inc"
+// the reference's own marching-cubes tables, from its source tree (include path set by the recipe)
+#include "MarchingCubesTables.h"
 
 // ------------------------------------------------------------------------------------ fibers
 namespace {
@@ -263,5 +266,34 @@ extern "C" int tfxr_expand_strands(const float* pos, const float* tan, int64_t v
         for (int k = 0; k < 4; ++k)
             for (int c = 0; c < 4; ++c) out[16 * id + 4 * k + c] = f[k][c];
     }
+    return 0;
+}
+
+// The reference's MARCHING_CUBES_EDGE_TABLE[256] and MARCHING_CUBES_TRIANGLE_TABLE[256*16].
+extern "C" int tfxr_mc_tables(int32_t* edge, int32_t* tri) {
+    for (int i = 0; i < 256; ++i) edge[i] = MARCHING_CUBES_EDGE_TABLE[i];
+    for (int i = 0; i < 256 * 16; ++i) tri[i] = MARCHING_CUBES_TRIANGLE_TABLE[i];
+    return 0;
+}
+
+// TressFXSDFMarchingCubes::Update (TressFXSDFMarchingCubes.cpp:168-232): InitializeMCVertices over
+// ceil(max / 64) groups, then RunMarchingCubesOnSdf over ceil(X*Y*Z / 64) groups, with the caller's
+// tables.  out = {position, normal}[maxVerts] (8 floats each); sdf = the finalized grid words.
+extern "C" int tfxr_marching_cubes(const uint32_t* sdf, int64_t allocCells, const SdfParamsF* g, float iso,
+                                   const int32_t* edge, const int32_t* tri, int maxVerts, float* out, int32_t* counter) {
+    using namespace ref_mc;
+    g_MarchingCubesSignedDistanceField.bind((void*)sdf, allocCells);
+    g_MarchingCubesTriangleVertices.bind(out, maxVerts);
+    g_NumMarchingCubesVertices.bind(counter, 1);
+    g_MarchingCubesEdgeTable.bind((void*)edge, 256);
+    g_MarchingCubesTriangleTable.bind((void*)tri, 256 * 16);
+    g_Origin = float4(g->origin[0], g->origin[1], g->origin[2], 0.0f);
+    g_CellSize = g->cellSize;
+    g_NumCellsX = g->nx; g_NumCellsY = g->ny; g_NumCellsZ = g->nz;
+    g_MaxMarchingCubesVertices = maxVerts;
+    g_MarchingCubesIsolevel = iso;
+    const int64_t cells = (int64_t)g->nx * g->ny * g->nz;
+    dispatch(InitializeMCVertices, (int)std::ceil((float)maxVerts / (float)kGroup), false);
+    dispatch(RunMarchingCubesOnSdf, (int)std::ceil((float)cells / (float)kGroup), false);
     return 0;
 }

@@ -239,6 +239,11 @@ struct HArray {
 };
 
 inline void InterlockedMin(uint& dest, uint value) { if (value < dest) dest = value; }
+// InterlockedAdd(dest, value, original): threads of a dispatch run one at a time here.
+template <class D, class V, class O> inline void InterlockedAdd(D& dest, V value, O& original) {
+    original = (O)dest;
+    dest = (D)(dest + value);
+}
 
 // Group barrier: provided by the fiber scheduler of the dispatch emulator.
 void GroupMemoryBarrierWithGroupSync();

@@ -19,6 +19,8 @@ The rewrites, in order:
      by what it uses from the other files: the TRESSFX_FLOAT_EPSILON define, MatrixMult and the two
      Safe_normalize overloads of TressFXUtilities.hlsl, and the cbuffer TressFXStrandParameters of
      TressFXRendering.hlsl; `.rgb` reads `.xyz` and `(TressFXVertex)0` value-initialises.
+ 10. for TressFXMarchingCubes.hlsl only the compute part between `//StartHLSL` and `//EndHLSL` is
+     kept; the vertex/pixel shaders after it draw the mesh.
 
 The output is wrapped in a namespace per shader file and compiled against hlsl_shim.h.
 """
@@ -34,6 +36,7 @@ SHADERS = {
     "ref_sdf": "src/Shaders/TressFXSDFCollision.hlsl",
     "ref_skin": "src/Shaders/TressFXBoneSkinning.hlsl",
     "ref_strands": "src/Shaders/TressFXStrands.hlsl",
+    "ref_mc": "src/Shaders/TressFXMarchingCubes.hlsl",
 }
 
 
@@ -95,6 +98,8 @@ def translate(text: str, name: str) -> str:
     s = text
     if name == "ref_skin":
         s = s.split("// visualization")[0]
+    if name == "ref_mc":
+        s = s.split("//StartHLSL TressFXMarchingCubesCS")[1].split("//EndHLSL")[0]
     s = re.sub(r"\[\[vk::binding\([^)]*\)\]\]", "", s)
     s = re.sub(r":\s*register\s*\([^)]*\)", "", s)
     s = re.sub(r"^\s*\[numthreads\([^)]*\)\]\s*$", "", s, flags=re.M)

@@ -886,3 +886,71 @@ extern "C" int tfxo_expand_strands(const float* pos, const float* tan, int64_t v
     }
     return 0;
 }
+
+// ============================================================================ marching cubes
+// RunMarchingCubesOnSdf (TressFXMarchingCubes.hlsl:147-280) over every cell in index order -- the order
+// in which a one-thread-at-a-time dispatch appends -- after InitializeMCVertices (:127-145).  The
+// tables are the caller's (the shader reads them from buffers).  Output: {position, normal} as 8
+// floats per vertex; *counter = every cube's reservation, as the shader's InterlockedAdd counter.
+namespace {
+const int kMcCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1}, {0, 1, 0}, {1, 1, 0}, {1, 1, 1}, {0, 1, 1}};
+const int kMcEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+}  // namespace
+
+extern "C" int tfxo_marching_cubes_f32(const float* sdf, const SdfParamsF* g, float iso, const int32_t* edgeTable,
+                                       const int32_t* triTable, int maxVerts, float* out, int32_t* counter) {
+    if (!sdf || !g || !edgeTable || !triTable || (!out && maxVerts > 0) || !counter || maxVerts < 0) return 1;
+    for (int i = 0; i < 256 * 16; ++i)
+        if (triTable[i] < -1 || triTable[i] > 11) return 2;
+    std::memset(out, 0, (size_t)maxVerts * 8 * sizeof(float));
+    const int X = g->nx, Y = g->ny, Z = g->nz;
+    const int64_t total = (int64_t)X * Y * Z;
+    int64_t count = 0;
+    for (int64_t idx = 0; idx < total; ++idx) {
+        const int z = (int)(idx / ((int64_t)X * Y)), rem = (int)(idx % ((int64_t)X * Y));
+        const int y = rem / X, x = rem % X;
+        if (!(x < X - 1) || !(y < Y - 1) || !(z < Z - 1)) continue;
+        float pos[8][3], s[8];
+        for (int k = 0; k < 8; ++k) {
+            const int cx = x + kMcCorner[k][0], cy = y + kMcCorner[k][1], cz = z + kMcCorner[k][2];
+            pos[k][0] = (float)cx * g->cellSize;
+            pos[k][1] = (float)cy * g->cellSize;
+            pos[k][2] = (float)cz * g->cellSize;
+            pos[k][0] = pos[k][0] + g->origin[0];
+            pos[k][1] = pos[k][1] + g->origin[1];
+            pos[k][2] = pos[k][2] + g->origin[2];
+            s[k] = sdf[(int64_t)X * Y * cz + (int64_t)X * cy + cx];
+        }
+        int cfg = 0;
+        for (int k = 0; k < 8; ++k)
+            if (s[k] < iso) cfg |= 1 << k;
+        if (!edgeTable[cfg]) continue;
+        float v[12][3] = {};
+        for (int e = 0; e < 12; ++e) {
+            if (!(edgeTable[cfg] & (1 << e))) continue;
+            const int a = kMcEdge[e][0], b = kMcEdge[e][1];
+            const float interp = (iso - s[a]) / (s[b] - s[a]);
+            for (int d = 0; d < 3; ++d) v[e][d] = pos[a][d] + (pos[b][d] - pos[a][d]) * interp;
+        }
+        int nv = 0;
+        while (nv < 16 && triTable[cfg * 16 + nv] != -1) ++nv;
+        const int64_t offset = count;
+        count += nv;
+        if (!(offset + nv < maxVerts)) continue;
+        for (int t = 0; t < nv / 3; ++t) {
+            const float* p[3];
+            for (int c = 0; c < 3; ++c) p[c] = v[triTable[cfg * 16 + 3 * t + c]];
+            const float a[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+            const float b[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+            const float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+            const float inv = 1.0f / std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            for (int c = 0; c < 3; ++c) {
+                float* o = out + 8 * (offset + 3 * t + c);
+                o[0] = p[c][0]; o[1] = p[c][1]; o[2] = p[c][2]; o[3] = 0.f;
+                o[4] = n[0] * inv; o[5] = n[1] * inv; o[6] = n[2] * inv; o[7] = 0.f;
+            }
+        }
+    }
+    *counter = (int32_t)count;
+    return 0;
+}

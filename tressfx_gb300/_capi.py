@@ -178,6 +178,15 @@ _PROTOS = {
     "tfx_sdf_write": (C.c_int, [P, P, C.c_size_t]),
     "tfx_sdf_get_buffer": (C.c_int, [P, C.POINTER(P), C.POINTER(C.c_size_t)]),
     "tfx_sdf_build_static": (C.c_int, [P, P, P, C.c_int, P, C.c_int, P]),
+    "tfx_mc_create": (C.c_int, [P, C.c_int, C.c_int64, C.POINTER(P)]),
+    "tfx_mc_destroy": (C.c_int, [P]),
+    "tfx_mc_default_tables": (C.c_int, [P, P]),
+    "tfx_mc_set_tables": (C.c_int, [P, P, P]),
+    "tfx_mc_set_iso_level": (C.c_int, [P, F32]),
+    "tfx_mc_update": (C.c_int, [P, P, C.POINTER(SdfGrid)]),
+    "tfx_mc_run": (C.c_int, [P, P, C.POINTER(SdfGrid)]),
+    "tfx_mc_get_buffers": (C.c_int, [P, C.POINTER(P), C.POINTER(P)]),
+    "tfx_mc_read": (C.c_int, [P, P, C.c_size_t, C.POINTER(C.c_int32)]),
     "tfx_mesh_create": (C.c_int, [P, P, C.c_int, P, C.c_int, P, C.POINTER(P)]),
     "tfx_mesh_destroy": (C.c_int, [P]),
     "tfx_mesh_skin": (C.c_int, [P, P, C.c_int]),

@@ -317,6 +317,67 @@ class SDFCollision:
             pass
 
 
+def mc_default_tables() -> tuple[np.ndarray, np.ndarray]:
+    """The library's marching-cubes tables: edge[256] and triangles[256, 16] (-1 terminated)."""
+    e = np.zeros(256, np.int32)
+    t = np.zeros((256, 16), np.int32)
+    check(A.lib().tfx_mc_default_tables(ptr(e), ptr(t)), "tfx_mc_default_tables")
+    return e, t
+
+
+class SDFMarchingCubes:
+    """TressFXSDFMarchingCubes: the iso-surface of a signed distance grid as a device triangle soup of
+    {float4 position, float4 normal} vertices, in cell-index order."""
+
+    def __init__(self, ctx: Context, max_vertices: int = 128 * 1024, max_cells: int = 1 << 21):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(A.lib().tfx_mc_create(ctx.handle, int(max_vertices), int(max_cells), C.byref(h)), "tfx_mc_create")
+        self.handle = h
+        self.max_vertices = int(max_vertices)
+
+    def set_tables(self, edge_table=None, tri_table=None) -> None:
+        if edge_table is None:
+            check(A.lib().tfx_mc_set_tables(self.handle, None, None), "tfx_mc_set_tables")
+            return
+        e = np.ascontiguousarray(edge_table, dtype=np.int32).reshape(256)
+        t = np.ascontiguousarray(tri_table, dtype=np.int32).reshape(256 * 16)
+        check(A.lib().tfx_mc_set_tables(self.handle, ptr(e), ptr(t)), "tfx_mc_set_tables")
+
+    def set_iso_level(self, iso_level_cells: float) -> None:
+        check(A.lib().tfx_mc_set_iso_level(self.handle, float(iso_level_cells)), "tfx_mc_set_iso_level")
+
+    def update(self, sdf: SDFCollision, grid: A.SdfGrid) -> None:
+        check(A.lib().tfx_mc_update(self.handle, sdf.handle, C.byref(grid)), "tfx_mc_update")
+
+    def run(self, sdf_device_ptr: int, grid: A.SdfGrid) -> None:
+        check(A.lib().tfx_mc_run(self.handle, sdf_device_ptr, C.byref(grid)), "tfx_mc_run")
+
+    def buffers(self) -> tuple[int, int]:
+        v, n = C.c_void_p(), C.c_void_p()
+        check(A.lib().tfx_mc_get_buffers(self.handle, C.byref(v), C.byref(n)), "tfx_mc_get_buffers")
+        return v.value, n.value
+
+    def read(self, vertices: int | None = None) -> tuple[np.ndarray, int]:
+        """(vertices[:vertices] as (N, 8) float32, the counter)."""
+        nv = self.max_vertices if vertices is None else int(vertices)
+        out = np.empty((nv, 8), np.float32)
+        cnt = C.c_int32()
+        check(A.lib().tfx_mc_read(self.handle, ptr(out), out.nbytes, C.byref(cnt)), "tfx_mc_read")
+        return out, cnt.value
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            A.lib().tfx_mc_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Batch:
     """tfx_batch: many hair objects and their SDFs advanced by one CUDA-graph launch per frame."""
 
