@@ -45,6 +45,8 @@ WORKLOADS = {
     "small": "plain small 2048x16, no SDF",
     "neural": "learned collision proxy: head mesh (20k tris) posed by 3 joints in +-40 deg, 20000x32 guides, "
               "MLP trained on 512 poses x 8192 samples of 128^3 grid SDFs",
+    "kernels": "head 20000x32 F=4 after 4 frames: SDF collision (forward / mixed differences, 64^3), strand quad "
+               "expansion (6.4M vertex ids), marching cubes of a 128^3 SDF of the skinned head mesh",
 }
 
 
@@ -437,6 +439,113 @@ def run_neural(args, base_cfg: dict, metric: str) -> dict:
     return line
 
 
+def run_kernels(args, base_cfg: dict) -> dict:
+    """The kernels of the rows around the hot path, each timed alone with CUDA events on the library's
+    stream and L2 flushed (a 1 GB write) before every launch: the two SDF collision variants, the
+    strand quad expansion and marching cubes.  Algorithmic bytes per launch: collision 32 B per vertex
+    (position and previous position read) + the grid once; expansion 32 B per vertex read + 64 B per
+    vertex id written (two ids per vertex); marching cubes 4 B per cell read + 32 B per vertex of the
+    max_vertices buffer written (triangles, then InitializeMCVertices' zeros)."""
+    import ctypes as C
+    import torch
+    from tressfx_gb300 import _capi as A
+    from tressfx_gb300._capi import check
+    from tressfx_gb300.api import Context, SDFCollision, SDFMarchingCubes
+    from tressfx_gb300.headless import FrameInputs, PlainPipeline
+    from tressfx_gb300.synthetic import margin_world
+    scene = make_scene("head")
+    obj = scene.objects[0]
+    ctx = Context(0)
+    pipe = PlainPipeline(ctx, scene)
+    for f in range(4):
+        pipe.step(f)
+    fin = FrameInputs(scene, 4)
+    pipe.prepare(fin)
+    g64 = fin.grids[0]
+    pipe.meshes[0].skin(fin.mesh_bones[0])
+    pipe.sdfs[0].update(g64)
+    h = pipe.hair[0]
+    V = h.num_vertices
+    margin = margin_world(obj, g64)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(256 << 20, dtype=torch.float32, device="cuda")   # 1 GB: also hides the host launch time
+    reps = min(max(args.steps, 5), 100)
+
+    def timed(fn) -> float:
+        for _ in range(3):
+            fn()
+        ctx.synchronize()
+        ctx.timestamps()
+        for i in range(reps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+            ctx.timestamp("a")
+            fn()
+            ctx.timestamp("b")
+        st = ctx.timestamps()
+        return sum(st[2 * i + 1][1] - st[2 * i][1] for i in range(reps)) / reps
+
+    peaks = load_peaks()
+    out = {}
+
+    def record(name, ms, units, unit, nbytes, **extra):
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = dict(ms=ms, value=units / (ms * 1e-3), unit=unit, algorithmic_bytes=nbytes, gbs=gbs,
+                         frac_of_measured_hbm=gbs / peaks["hbm_gbs"], **extra)
+
+    cells64 = g64.num_cells_x * g64.num_cells_y * g64.num_cells_z
+    record("sdf_collide_forward", timed(lambda: pipe.sdfs[0].collide(h, g64, margin)), V, "vertices/s",
+           32 * V + 4 * cells64, grid=[g64.num_cells_x, g64.num_cells_y, g64.num_cells_z])
+    record("sdf_collide_mixed", timed(lambda: pipe.sdfs[0].collide_mixed(h, g64, margin)), V, "vertices/s",
+           32 * V + 4 * cells64, grid=[g64.num_cells_x, g64.num_cells_y, g64.num_cells_z])
+    # strand quad expansion
+    sp = A.StrandParams()
+    for k in range(4):
+        sp.mat_base_color[k], sp.mat_tip_color[k] = 0.4, 0.8
+    sp.tip_percentage, sp.strand_uv_tiling_factor, sp.fiber_ratio, sp.fiber_radius = 0.5, 1.0, 0.06, 0.002
+    sp.num_vertices_per_strand, sp.enable_thin_tip = scene.objects[0].asset.verts_per_strand, 1
+    eye = (C.c_float * 3)(0.0, 1.7, 0.9)
+    win = (C.c_float * 2)(1920.0, 1080.0)
+    vp = (C.c_float * 16)(*[1.0 if i % 5 == 0 else 0.0 for i in range(16)])
+    ebuf = torch.empty((2 * V, 16), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    record("expand_strands", timed(lambda: check(A.lib().tfx_hair_expand_strands(h.handle, C.byref(sp), eye, win, vp, 0,
+                                                                                ebuf.data_ptr()))),
+           2 * V, "vertex ids/s", 32 * V + 128 * V)
+    # marching cubes of a 128^3 grid of the skinned head mesh
+    sk = pipe.meshes[0].read_skinned().reshape(-1, 8)[:, :3]
+    lo, hi = sk.min(0), sk.max(0)
+    cell = float(np.float32((hi - lo).max() / 120.0))
+    g128 = A.SdfGrid()
+    for k in range(3):
+        g128.origin[k] = float(lo[k] - 4 * cell)
+    g128.cell_size = cell
+    g128.num_cells_x = g128.num_cells_y = g128.num_cells_z = 128
+    sdf128 = SDFCollision(ctx, 128 ** 3)
+    sdf128.bind_mesh(pipe.meshes[0])
+    sdf128.update(g128)
+    maxv = 1 << 20
+    mc = SDFMarchingCubes(ctx, maxv, 128 ** 3)
+    mc.set_iso_level(0.0)
+    ms = timed(lambda: mc.update(sdf128, g128))
+    _, count = mc.read(0)
+    record("marching_cubes", ms, 128 ** 3, "cells/s", 4 * 128 ** 3 + 32 * maxv, vertices=count, max_vertices=maxv,
+           grid=[128, 128, 128])
+    mc.close()
+    sdf128.close()
+    pipe.close()
+    ctx.close()
+    m = out["marching_cubes"]
+    return {"metric": "SDF cells/s (marching cubes)", "value": m["value"], "unit": "cells/s", "n_gpus": 1,
+            "steps": reps, "warmup": 3, "ms_per_step": m["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": dict(base_cfg, l2="L2 flushed (1 GB write) before every timed launch"),
+            "roofline": {"bound": "hbm", "kernel": "k_mc_count + k_mc_write", "achieved": m["gbs"],
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": m["frac_of_measured_hbm"], "traffic": None,
+                         "peak_source": peaks["source"]},
+            "kernels": out}
+
+
 # ------------------------------------------------------------------------------------------ main
 def main() -> None:
     ap = argparse.ArgumentParser()
@@ -480,9 +589,10 @@ def main() -> None:
             dist.destroy_process_group()
         return
 
-    if args.config == "neural":
+    if args.config in ("neural", "kernels"):
         if rank == 0:
-            print(json.dumps(run_neural(args, base_cfg, metric)), flush=True)
+            run = run_neural if args.config == "neural" else (lambda a, c, m: run_kernels(a, c))
+            print(json.dumps(run(args, base_cfg, metric)), flush=True)
         if dist is not None:
             dist.destroy_process_group()
         return

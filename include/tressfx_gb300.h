@@ -282,7 +282,7 @@ int tfx_sdf_build_static(tfx_context ctx, const tfx_sdf_grid* grid, const void* 
  * [max_vertices] (StandardVertex of TressFXMarchingCubes.hlsl:33-37), headless. */
 typedef struct tfx_mc_t* tfx_mc;
 /* Constructor + Initialize (TressFXSDFMarchingCubes.cpp:27-118): the vertex buffer (128*1024 vertices
- * in the reference), the counter, and scratch for grids of up to max_cells cells (< 2^31 - 4096).  The
+ * in the reference), the counter, and scratch for grids of up to max_cells cells (< 2^31 - 256).  The
  * tables start as tfx_mc_default_tables'; the iso level starts at 0. */
 int tfx_mc_create(tfx_context ctx, int max_vertices, int64_t max_cells, tfx_mc* out);
 int tfx_mc_destroy(tfx_mc mc);

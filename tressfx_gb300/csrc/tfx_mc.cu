@@ -5,12 +5,14 @@
 // The reference appends each cube's triangles at an atomically reserved offset, so its vertex order
 // changes from run to run.  Here the offsets are an exclusive prefix sum of the cubes' vertex counts
 // in cell-index order -- the order a one-thread-at-a-time dispatch of the shader produces -- so the
-// buffer is deterministic and bit-comparable.  Two passes over the grid:
-//   k_mc_count: 4096 cells per block (16 per thread, coalesced along x), one vertex-count sum per block;
-//   k_mc_write: each block sums the counts of the blocks before it, scans its own cells and writes
-//               the triangles of every cube whose range ends before max_vertices (the shader's
-//               `offset + num < max`), zeros what InitializeMCVertices would leave zero, and block 0
-//               stores the total (the shader's counter, which also counts cubes that did not fit).
+// buffer is deterministic and bit-comparable.  Three launches:
+//   k_mc_count: one cell per thread, the vertex count every block of 256 cells reserves;
+//   k_mc_scan:  one block, the exclusive prefix of those counts (64-bit) and the total (the shader's
+//               counter, which also counts cubes that did not fit);
+//   k_mc_write: each block rescans its cells in shared memory and spreads its output vertices over its
+//               threads, one 32-byte vertex per thread (coalesced stores); a cube is written only if
+//               its range ends below max_vertices (the shader's `offset + num < max`), and whatever
+//               InitializeMCVertices would leave zero is zeroed.
 // The grid (a few MB) stays in L2 between the passes.
 #include <cstring>
 #include <new>
@@ -30,9 +32,8 @@ struct McTables {
 
 namespace {
 
-constexpr int kMcThreads = 256;
-constexpr int kMcPerThread = 16;
-constexpr int kMcBlockCells = kMcThreads * kMcPerThread;
+constexpr int kMcThreads = 256;       // cells of a block, one per thread
+constexpr int kMcScanThreads = 1024;
 
 // Corner k of a cube sits at cell + kCorner[k] (TressFXMarchingCubes.hlsl:165-173); edge e joins the
 // corners kEdgeA[e] -> kEdgeB[e], in the argument order of its VertexLerp call (:211-222).
@@ -42,98 +43,76 @@ __constant__ int8_t kCornerZ[8] = {0, 0, 1, 1, 0, 0, 1, 1};
 __constant__ int8_t kEdgeA[12] = {0, 1, 2, 3, 4, 5, 6, 7, 0, 1, 2, 3};
 __constant__ int8_t kEdgeB[12] = {1, 2, 3, 0, 5, 6, 7, 4, 4, 5, 6, 7};
 
-struct McCell {
-    int x, y, z;
-    float s[8];
-    int config;          // cubeIndex; -1 for cells on the upper faces of the grid
-};
-
-__device__ __forceinline__ McCell mc_cell(const float* __restrict__ sdf, const SdfGrid& g, int index, float iso) {
-    McCell c;
+// The cell of linear index `index` (x fastest), as GetSdfCellPositionFromIndex computes it.
+__device__ __forceinline__ int3 mc_cell_xyz(const SdfGrid& g, int index) {
     const uint32_t perLine = (uint32_t)g.nx, perPlane = (uint32_t)(g.nx * g.ny);
     const uint32_t u = (uint32_t)index;
-    c.z = (int)(u / perPlane);
     const uint32_t rem = u % perPlane;
-    c.y = (int)(rem / perLine);
-    c.x = (int)(rem % perLine);
-    c.config = -1;
-    if (c.x >= g.nx - 1 || c.y >= g.ny - 1 || c.z >= g.nz - 1) return c;
+    return make_int3((int)(rem % perLine), (int)(rem / perLine), (int)(u / perPlane));
+}
+
+// The eight corner values of cube `c` and its cubeIndex; -1 for cells on the upper faces of the grid.
+__device__ __forceinline__ int mc_config(const float* __restrict__ sdf, const SdfGrid& g, int3 c, float iso, float s[8]) {
+    if (c.x >= g.nx - 1 || c.y >= g.ny - 1 || c.z >= g.nz - 1) return -1;
     const int plane = g.nx * g.ny;
     const float* p = sdf + (plane * c.z + g.nx * c.y + c.x);
     // corners 0..7: (0,0,0) (1,0,0) (1,0,1) (0,0,1) (0,1,0) (1,1,0) (1,1,1) (0,1,1)
-    c.s[0] = __ldg(p);
-    c.s[1] = __ldg(p + 1);
-    c.s[2] = __ldg(p + plane + 1);
-    c.s[3] = __ldg(p + plane);
-    c.s[4] = __ldg(p + g.nx);
-    c.s[5] = __ldg(p + g.nx + 1);
-    c.s[6] = __ldg(p + plane + g.nx + 1);
-    c.s[7] = __ldg(p + plane + g.nx);
+    s[0] = __ldg(p);
+    s[1] = __ldg(p + 1);
+    s[2] = __ldg(p + plane + 1);
+    s[3] = __ldg(p + plane);
+    s[4] = __ldg(p + g.nx);
+    s[5] = __ldg(p + g.nx + 1);
+    s[6] = __ldg(p + plane + g.nx + 1);
+    s[7] = __ldg(p + plane + g.nx);
     int cfg = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-        if (c.s[k] < iso) cfg |= 1 << k;
-    c.config = cfg;
-    return c;
+        if (s[k] < iso) cfg |= 1 << k;
+    return cfg;
 }
 
-// GetSdfCellPosition: float3(cell) * cellSize, then + origin.
-__device__ __forceinline__ float3 mc_corner(const McCell& c, const SdfGrid& g, int k) {
-    float3 p = make_float3((float)(c.x + kCornerX[k]) * g.cell, (float)(c.y + kCornerY[k]) * g.cell,
-                           (float)(c.z + kCornerZ[k]) * g.cell);
+// GetSdfCellPosition of corner k: float3(cell + offset) * cellSize, then + origin.
+__device__ __forceinline__ float3 mc_corner(int3 c, const SdfGrid& g, int k) {
+    const float3 p = make_float3((float)(c.x + kCornerX[k]) * g.cell, (float)(c.y + kCornerY[k]) * g.cell,
+                                 (float)(c.z + kCornerZ[k]) * g.cell);
     return make_float3(p.x + g.ox, p.y + g.oy, p.z + g.oz);
 }
 
-// VertexLerp: p1 + (p2 - p1) * ((iso - s1) / (s2 - s1)).
-__device__ __forceinline__ float3 mc_edge_vertex(const McCell& c, const SdfGrid& g, int e, float iso) {
+// VertexLerp on edge e: p1 + (p2 - p1) * ((iso - s1) / (s2 - s1)); s = the cube's corner values.
+__device__ __forceinline__ float3 mc_edge_vertex(int3 c, const SdfGrid& g, const float* s, int e, float iso) {
     const int a = kEdgeA[e], b = kEdgeB[e];
-    float sa = 0.f, sb = 0.f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        sa = (k == a) ? c.s[k] : sa;
-        sb = (k == b) ? c.s[k] : sb;
-    }
+    const float sa = s[a * kMcThreads], sb = s[b * kMcThreads];
     const float interp = (iso - sa) / (sb - sa);
     const float3 p1 = mc_corner(c, g, a), p2 = mc_corner(c, g, b);
     return make_float3(p1.x + (p2.x - p1.x) * interp, p1.y + (p2.y - p1.y) * interp, p1.z + (p2.z - p1.z) * interp);
 }
 
-__device__ __forceinline__ int block_sum(int v, int* red) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+// Exclusive scan of one value per thread over a block of NT threads; *total receives the sum.
+template <int NT, class T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* red, T* total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    int t = 0;
-#pragma unroll
-    for (int w = 0; w < kMcThreads / 32; ++w) t += red[w];
-    return t;
-}
-
-// Exclusive scan over the block; *total receives the block's sum.
-__device__ __forceinline__ int block_exclusive_scan(int v, int* red, int* total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int incl = v;
+    T incl = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        const T n = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += n;
     }
     __syncthreads();
     if (lane == 31) red[warp] = incl;
     __syncthreads();
-    int before = 0, all = 0;
+    T before = 0, all = 0;
 #pragma unroll
-    for (int w = 0; w < kMcThreads / 32; ++w) {
-        const int t = red[w];
-        before += (w < warp) ? t : 0;
+    for (int w = 0; w < NT / 32; ++w) {
+        const T t = red[w];
+        before += (w < warp) ? t : (T)0;
         all += t;
     }
     *total = all;
     return before + incl - v;
 }
 
+// Pass 1: the vertices every block of 256 cells reserves.
 __global__ void __launch_bounds__(kMcThreads) k_mc_count(const float* __restrict__ sdf, SdfGrid g, float iso,
                                                          const McTables* __restrict__ T, int totalCells,
                                                          int* __restrict__ blockSums) {
@@ -141,17 +120,43 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_count(const float* __restrict
     __shared__ int red[kMcThreads / 32];
     cnt[threadIdx.x] = T->count[threadIdx.x];
     __syncthreads();
-    const int base = blockIdx.x * kMcBlockCells;
-    int sum = 0;
-#pragma unroll 4
-    for (int j = 0; j < kMcPerThread; ++j) {
-        const int idx = base + j * kMcThreads + (int)threadIdx.x;
-        if (idx >= totalCells) break;
-        const McCell c = mc_cell(sdf, g, idx, iso);
-        if (c.config >= 0) sum += cnt[c.config];
+    const int idx = blockIdx.x * kMcThreads + (int)threadIdx.x;
+    int nv = 0;
+    if (idx < totalCells) {
+        float s[8];
+        const int cfg = mc_config(sdf, g, mc_cell_xyz(g, idx), iso, s);
+        nv = cfg >= 0 ? cnt[cfg] : 0;
     }
-    const int t = block_sum(sum, red);
-    if (threadIdx.x == 0) blockSums[blockIdx.x] = t;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = nv;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+#pragma unroll
+        for (int w = 0; w < kMcThreads / 32; ++w) t += red[w];
+        blockSums[blockIdx.x] = t;
+    }
+}
+
+// Pass 2 (one block): exclusive prefix of the block sums in 64 bits; blockOff[nb] = the total, and
+// the counter (an int, as in the shader) its low 32 bits.
+__global__ void __launch_bounds__(kMcScanThreads) k_mc_scan(const int* __restrict__ blockSums, int nb,
+                                                            long long* __restrict__ blockOff, int* __restrict__ counter) {
+    __shared__ long long red[kMcScanThreads / 32];
+    long long carry = 0;
+    for (int base = 0; base < nb; base += kMcScanThreads) {
+        const int b = base + (int)threadIdx.x;
+        const long long v = b < nb ? blockSums[b] : 0;
+        long long total;
+        const long long ex = block_exclusive_scan<kMcScanThreads>(v, red, &total);
+        if (b < nb) blockOff[b] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        blockOff[nb] = carry;
+        *counter = (int)carry;
+    }
 }
 
 __device__ __forceinline__ void mc_zero(float4* out, long long v) {
@@ -159,108 +164,97 @@ __device__ __forceinline__ void mc_zero(float4* out, long long v) {
     out[2 * v + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// Pass 3: the block's cells are scanned in shared memory, then its output vertices are spread over
+// the threads (thread k writes vertex k, 32 contiguous bytes: coalesced); each thread evaluates the
+// three edge vertices and the normal of its vertex's triangle.  A cube that does not end below
+// maxVerts gets zeros in its range (below maxVerts), and so do the vertices past a count that is not
+// a multiple of 3.  Vertices [total, maxVerts) are zeroed by all blocks together.
 __global__ void __launch_bounds__(kMcThreads) k_mc_write(const float* __restrict__ sdf, SdfGrid g, float iso,
                                                          const McTables* __restrict__ T, int totalCells,
-                                                         const int* __restrict__ blockSums, int numBlocks, int maxVerts,
-                                                         float4* __restrict__ out, int* __restrict__ counter) {
-    __shared__ int cnt[256];
+                                                         const int* __restrict__ blockSums,
+                                                         const long long* __restrict__ blockOff, int nb, int maxVerts,
+                                                         float4* __restrict__ out) {
+    __shared__ float cs[8 * kMcThreads];      // corner values, [corner][cell]
+    __shared__ int ccfg[kMcThreads];
+    __shared__ int cstart[kMcThreads + 1];
     __shared__ int red[kMcThreads / 32];
-    cnt[threadIdx.x] = T->count[threadIdx.x];
-    // prefix of the earlier blocks and the grand total, summed in 64 bits (the counter, an int as in
-    // the shader, receives the low 32 bits)
-    long long before = 0, all = 0;
-    for (int b = threadIdx.x; b < numBlocks; b += kMcThreads) {
-        const int s = __ldg(blockSums + b);
-        all += s;
-        before += (b < (int)blockIdx.x) ? s : 0;
-    }
-    {
-        __shared__ long long red2[2][kMcThreads / 32];
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            before += __shfl_xor_sync(0xffffffffu, before, o);
-            all += __shfl_xor_sync(0xffffffffu, all, o);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            red2[0][threadIdx.x >> 5] = before;
-            red2[1][threadIdx.x >> 5] = all;
-        }
-        __syncthreads();
-        before = 0;
-        all = 0;
-#pragma unroll
-        for (int w = 0; w < kMcThreads / 32; ++w) {
-            before += red2[0][w];
-            all += red2[1][w];
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) *counter = (int)all;
-    // vertices past the last reservation keep InitializeMCVertices' zeros
-    for (long long v = all + (long long)blockIdx.x * kMcThreads + threadIdx.x; v < maxVerts;
+    const long long total = __ldg(blockOff + nb);
+    for (long long v = total + (long long)blockIdx.x * kMcThreads + threadIdx.x; v < maxVerts;
          v += (long long)gridDim.x * kMcThreads)
         mc_zero(out, v);
     const int mine = __ldg(blockSums + blockIdx.x);
-    if (mine == 0 || before >= maxVerts) {
-        // nothing of this block fits: zero the part of its reservations below maxVerts
-        if (mine != 0)
-            for (long long v = before + threadIdx.x; v < before + mine && v < maxVerts; v += kMcThreads) mc_zero(out, v);
-        return;
-    }
-    const int base = blockIdx.x * kMcBlockCells;
-    long long running = before;
-    for (int j = 0; j < kMcPerThread; ++j) {
-        const int idx = base + j * kMcThreads + (int)threadIdx.x;
-        McCell c;
-        c.config = -1;
-        if (idx < totalCells) c = mc_cell(sdf, g, idx, iso);
-        const int nv = c.config >= 0 ? cnt[c.config] : 0;
-        int rowTotal;
-        const long long offset = running + block_exclusive_scan(nv, red, &rowTotal);
-        running += rowTotal;
-        if (nv == 0) continue;
-        if (offset + nv < maxVerts) {
-            const int* tri = T->tri + 16 * c.config;
-            const int ntri = nv / 3;
-            for (int t = 0; t < ntri; ++t) {
-                const float3 v0 = mc_edge_vertex(c, g, __ldg(tri + 3 * t), iso);
-                const float3 v1 = mc_edge_vertex(c, g, __ldg(tri + 3 * t + 1), iso);
-                const float3 v2 = mc_edge_vertex(c, g, __ldg(tri + 3 * t + 2), iso);
-                // normalize(cross(v1 - v0, v2 - v0)) = n * (1 / sqrt(dot(n, n)))
-                const float3 a = make_float3(v1.x - v0.x, v1.y - v0.y, v1.z - v0.z);
-                const float3 b = make_float3(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z);
-                const float3 n = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-                const float inv = 1.0f / sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
-                const float4 nn = make_float4(n.x * inv, n.y * inv, n.z * inv, 0.f);
-                float4* o = out + 2 * (offset + 3 * t);
-                o[0] = make_float4(v0.x, v0.y, v0.z, 0.f);
-                o[1] = nn;
-                o[2] = make_float4(v1.x, v1.y, v1.z, 0.f);
-                o[3] = nn;
-                o[4] = make_float4(v2.x, v2.y, v2.z, 0.f);
-                o[5] = nn;
-            }
-            for (int k = 3 * ntri; k < nv; ++k) mc_zero(out, offset + k);   // a count not divisible by 3
-        } else {
-            for (long long v = offset; v < offset + nv && v < maxVerts; ++v) mc_zero(out, v);
+    const long long off = __ldg(blockOff + blockIdx.x);
+    if (mine == 0 || off >= maxVerts) return;
+    const int cell0 = blockIdx.x * kMcThreads;
+    const int idx = cell0 + (int)threadIdx.x;
+    int nv = 0, cfg = -1;
+    if (idx < totalCells) {
+        float s[8];
+        cfg = mc_config(sdf, g, mc_cell_xyz(g, idx), iso, s);
+        if (cfg >= 0) {
+            nv = __ldg(T->count + cfg);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cs[k * kMcThreads + threadIdx.x] = s[k];
         }
+    }
+    ccfg[threadIdx.x] = cfg;
+    int sum;
+    const int ex = block_exclusive_scan<kMcThreads>(nv, red, &sum);
+    cstart[threadIdx.x] = ex;
+    if (threadIdx.x == 0) cstart[kMcThreads] = sum;
+    __syncthreads();
+    for (int k = threadIdx.x; k < mine; k += kMcThreads) {
+        const long long v = off + k;
+        if (v >= maxVerts) break;
+        // the cube holding vertex k: the last c with cstart[c] <= k (counts of 0 repeat a start)
+        int lo = 0, hi = kMcThreads - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (cstart[mid] <= k) lo = mid; else hi = mid - 1;
+        }
+        const int c = lo;
+        const int r = k - cstart[c];
+        const int n = cstart[c + 1] - cstart[c];
+        if (!(off + cstart[c] + n < maxVerts) || r >= 3 * (n / 3)) {
+            mc_zero(out, v);
+            continue;
+        }
+        const int cf = ccfg[c];
+        const int3 xyz = mc_cell_xyz(g, cell0 + c);
+        const int* tri = T->tri + 16 * cf + 3 * (r / 3);
+        const float* s = cs + c;
+        const float3 v0 = mc_edge_vertex(xyz, g, s, __ldg(tri), iso);
+        const float3 v1 = mc_edge_vertex(xyz, g, s, __ldg(tri + 1), iso);
+        const float3 v2 = mc_edge_vertex(xyz, g, s, __ldg(tri + 2), iso);
+        // normalize(cross(v1 - v0, v2 - v0)) = n * (1 / sqrt(dot(n, n)))
+        const float3 a = make_float3(v1.x - v0.x, v1.y - v0.y, v1.z - v0.z);
+        const float3 b = make_float3(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z);
+        const float3 nn = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+        const float inv = 1.0f / sqrtf(nn.x * nn.x + nn.y * nn.y + nn.z * nn.z);
+        const int corner = r % 3;
+        const float3 pv = corner == 0 ? v0 : (corner == 1 ? v1 : v2);
+        out[2 * v] = make_float4(pv.x, pv.y, pv.z, 0.f);
+        out[2 * v + 1] = make_float4(nn.x * inv, nn.y * inv, nn.z * inv, 0.f);
     }
 }
 
 }  // namespace
 
-int mc_num_blocks(long long cells) { return (int)((cells + kMcBlockCells - 1) / kMcBlockCells); }
+int mc_num_blocks(long long cells) { return (int)((cells + kMcThreads - 1) / kMcThreads); }
+size_t mc_scratch_bytes(long long cells) {
+    const size_t nb = (size_t)mc_num_blocks(cells);
+    return ((nb * sizeof(int) + 15) & ~(size_t)15) + (nb + 1) * sizeof(long long);
+}
 
 cudaError_t launch_marching_cubes(const float* sdf, const SdfGrid& g, float iso, const McTables* tables, int maxVerts,
-                                  int* blockSums, float4* out, int* counter, cudaStream_t s) {
+                                  void* scratch, float4* out, int* counter, cudaStream_t s) {
     const long long cells = (long long)g.nx * g.ny * g.nz;
     const int nb = mc_num_blocks(cells);
-    if (nb == 0) {
-        cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
-        if (e == cudaSuccess && maxVerts > 0) e = cudaMemsetAsync(out, 0, (size_t)maxVerts * 32, s);
-        return e;
-    }
+    int* blockSums = (int*)scratch;
+    long long* blockOff = (long long*)((char*)scratch + (((size_t)nb * sizeof(int) + 15) & ~(size_t)15));
     k_mc_count<<<nb, kMcThreads, 0, s>>>(sdf, g, iso, tables, (int)cells, blockSums);
-    k_mc_write<<<nb, kMcThreads, 0, s>>>(sdf, g, iso, tables, (int)cells, blockSums, nb, maxVerts, out, counter);
+    k_mc_scan<<<1, kMcScanThreads, 0, s>>>(blockSums, nb, blockOff, counter);
+    k_mc_write<<<nb, kMcThreads, 0, s>>>(sdf, g, iso, tables, (int)cells, blockSums, blockOff, nb, maxVerts, out);
     return cudaGetLastError();
 }
 
@@ -341,7 +335,7 @@ struct tfx_mc_t {
     float4* verts = nullptr;     // {position, normal}[maxVerts]
     int* counter = nullptr;
     McTables* tables = nullptr;
-    int* blockSums = nullptr;
+    void* scratch = nullptr;      // block sums + block offsets
 };
 
 static void mc_count_table(const int32_t* edge, const int32_t* tri, McTables* T) {
@@ -384,7 +378,7 @@ extern "C" int tfx_mc_set_tables(tfx_mc mc, const int32_t* edge_table, const int
 extern "C" int tfx_mc_create(tfx_context ctx, int max_vertices, int64_t max_cells, tfx_mc* out) {
     if (!out) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_mc_create: out is null");
     *out = nullptr;
-    if (!ctx || max_vertices < 0 || max_cells <= 0 || max_cells > 0x7fffffffLL - kMcBlockCells)
+    if (!ctx || max_vertices < 0 || max_cells <= 0 || max_cells > 0x7fffffffLL - kMcThreads)
         return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_mc_create: max_vertices %d max_cells %lld", max_vertices,
                     (long long)max_cells);
     TFX_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -395,7 +389,7 @@ extern "C" int tfx_mc_create(tfx_context ctx, int max_vertices, int64_t max_cell
     h->maxCells = max_cells;
     const size_t vb = ((size_t)max_vertices * 32 + 255) & ~(size_t)255;
     const size_t tb = (sizeof(McTables) + 255) & ~(size_t)255;
-    const size_t bb = (size_t)mc_num_blocks(max_cells) * sizeof(int);
+    const size_t bb = mc_scratch_bytes(max_cells);
     const size_t total = vb + 256 + tb + bb;
     cudaError_t e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) {
@@ -406,7 +400,7 @@ extern "C" int tfx_mc_create(tfx_context ctx, int max_vertices, int64_t max_cell
     h->verts = (float4*)p;
     h->counter = (int*)(p + vb);
     h->tables = (McTables*)(p + vb + 256);
-    h->blockSums = (int*)(p + vb + 256 + tb);
+    h->scratch = p + vb + 256 + tb;
     context_retain(ctx);
     // InitializeMCVertices before the first Update: zero vertices, zero counter
     e = cudaMemsetAsync(h->arena, 0, vb + 256, ctx->stream);
@@ -454,7 +448,7 @@ extern "C" int tfx_mc_run(tfx_mc mc, const float* sdf_device, const tfx_sdf_grid
     // g_MarchingCubesIsolevel = m_CellSize * m_SDFIsoLevel (TressFXSDFMarchingCubes.cpp:191)
     const float iso = grid->cell_size * mc->isoLevel;
     TFX_CUDA(cudaSetDevice(mc->ctx->device), "cudaSetDevice");
-    cudaError_t e = launch_marching_cubes(sdf_device, g, iso, mc->tables, mc->maxVerts, mc->blockSums, mc->verts,
+    cudaError_t e = launch_marching_cubes(sdf_device, g, iso, mc->tables, mc->maxVerts, mc->scratch, mc->verts,
                                           mc->counter, mc->ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "marching cubes launch");
     return TFX_OK;
