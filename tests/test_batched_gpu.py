@@ -156,3 +156,23 @@ def test_batched_options_bit_exact(ctx, expanded, overlap):
             gpu.batch.set_option(gpu.batch.SDF_BLOCK, 100)
     finally:
         gpu.close()
+
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("follows", [2, 4, 40])
+def test_batched_follow_collide_many_contacts_bit_exact(ctx, follows):
+    """The follow-hair + collision kernel with a wide margin (most vertices near the scalp collide) and
+    with more follow hairs than a warp has lanes: the oracle's buffers, bit for bit."""
+    sc = scene_head(seed=29, num_guides=96 if follows > 31 else 300, n=16, follows=follows, triangles=2500,
+                    sdf_cells=40, frames=5)
+    sc.objects[0].collision_margin_cells = 5.0
+    gpu = BatchedPipeline(ctx, sc)
+    try:
+        ora = OraclePipeline(sc)
+        for f in range(5):
+            fin = gpu.step(f)
+            ora.step(fin)
+        assert_same(gpu.hair[0], ora.hair[0], f"follows={follows}")
+    finally:
+        gpu.close()

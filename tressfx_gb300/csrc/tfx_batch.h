@@ -67,6 +67,7 @@ struct FollowLaunch {
     const BatchObject* objs;
     const WorkItem* items;
     int numItems;
+    int chunks;      // chunks per work item (1 .. follow_max_chunks_per_item(n))
 };
 
 struct SdfBatchLaunch {
@@ -86,6 +87,7 @@ bool fused_config_valid(int n, int vpl);
 int fused_smem_bytes(int n, int vpl, int warps);
 int fused_blocks_per_sm(int n, int vpl, int warps);
 int fused_group_size(int n);
+int follow_max_chunks_per_item(int n);   // 256-vertex chunks a work item can be cut into
 int follow_blocks_per_sm(int n);
 
 }  // namespace tfx

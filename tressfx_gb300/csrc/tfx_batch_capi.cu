@@ -32,7 +32,8 @@ struct BatchClass {
     int n = 0;
     int vpl = 1, warps = 8, blocks = 1;
     int perSMCap = 0;            // resident strand blocks per SM allowed (0 = as many as fit)
-    int followBlocks = 1;        // grid of k_follow_collide
+    int followBlocks = 1;        // grid of k_follow_collide (persistent over the chunks)
+    int followChunks = 1;        // chunks per group in k_follow_collide
     std::vector<WorkItem> hostItems;
     WorkItem* items = nullptr;  // device
     int numItems = 0;
@@ -200,8 +201,10 @@ static int size_class(tfx_batch b, BatchClass& c) {
         return fail(TFX_ERR_CUDA, "tfx_batch: fused kernel n=%d vpl=%d with %d warps cannot be resident", c.n, c.vpl, c.warps);
     if (c.perSMCap > 0) perSM = std::min(perSM, c.perSMCap);
     c.blocks = std::max(1, std::min(perSM * b->ctx->numSMs, c.numItems));
-    const int fpSM = std::max(1, follow_blocks_per_sm(c.n));
-    c.followBlocks = std::max(1, std::min(fpSM * b->ctx->numSMs, c.numItems));
+    // follow/collide: whole groups when every resident block gets at least four, else the smallest chunks
+    const int fResident = std::max(1, follow_blocks_per_sm(c.n)) * b->ctx->numSMs;
+    c.followChunks = c.numItems >= 4 * fResident ? 1 : follow_max_chunks_per_item(c.n);
+    c.followBlocks = std::max(1, std::min(fResident, c.numItems * c.followChunks));
     return TFX_OK;
 }
 
@@ -224,7 +227,7 @@ static int launch_strands(tfx_batch b, BatchClass& c, cudaStream_t s) {
 }
 
 static int launch_follows(tfx_batch b, BatchClass& c, cudaStream_t s) {
-    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems};
+    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems, c.followChunks};
     cudaError_t e = launch_follow_collide(fl, s);
     return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: follow/collide launch");
 }

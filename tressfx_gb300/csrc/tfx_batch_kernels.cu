@@ -572,6 +572,7 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
 // GetSignedDistance + TrilinearInterpolate (TressFXSDFCollision.hlsl:414-527) on the corner-expanded
 // grid: the same cell, bounds test, corner values and interpolation as sdf_lookup.
 __device__ __forceinline__ float sdf_lookup8(const float4* __restrict__ sdf8, const SdfGrid& g, float3 p) {
+    if (sdf_surely_outside(g, p)) return 1e10f;
     const int3 gc = sdf_coords(g, p);
     if (!(0 <= gc.x && gc.x < g.nx - 2) || !(0 <= gc.y && gc.y < g.ny - 2) || !(0 <= gc.z && gc.z < g.nz - 2))
         return 1e10f;
@@ -605,6 +606,113 @@ __device__ __forceinline__ bool sdf_collide_from8(const float4* __restrict__ sdf
     return false;
 }
 
+// The part of the collision after the first lookup (the vertices within the margin).
+__device__ __forceinline__ bool collide_near(const float* __restrict__ sdf, const float4* __restrict__ sdf8,
+                                             const SdfGrid& g, float margin, float3 p, float distance, float3* proj) {
+    float3 q = p;
+    const bool hit = sdf8 ? sdf_collide_from8(sdf8, g, margin, p, distance, q) : sdf_collide_from(sdf, g, margin, p, distance, q);
+    *proj = q;
+    return hit;
+}
+
+// What the vertices of one group share: the object's buffers, SDF, grid, margin, tip separation.
+struct FollowGroup {
+    HairView h;
+    const float* sdf;
+    const float4* sdf8;
+    SdfGrid sg;
+    float margin, tip;
+    int firstStrand;     // first strand of the group (guide strands and their follows)
+};
+
+__device__ __forceinline__ bool follow_group(const BatchObject& ob, const WorkItem& wi, FollowGroup& fg) {
+    fg.h = ob.hair;
+    fg.sdf = ob.sdf;
+    fg.sdf8 = ob.sdf8;
+    if (fg.h.F == 0 && !fg.sdf) return false;
+    fg.sg = SdfGrid{0.f, 0.f, 0.f, 1.f, 0, 0, 0, 0};
+    fg.margin = 0.0f;
+    if (fg.sdf) { fg.sg = ob.sdfFrame->grid; fg.margin = ob.sdfFrame->margin; }
+    fg.tip = ob.consts->tipSeparation;
+    fg.firstStrand = wi.firstGuide * (fg.h.F + 1);
+    return true;
+}
+
+// Guide vertex e of a group: its follow vertices and the collision of all of them.
+template <int N>
+__device__ __forceinline__ void follow_collide_vertex(const FollowGroup& fg, int e) {
+    constexpr int U = 4;   // the near-vertex loop below selects among exactly four
+    constexpr float kInvN = 1.0f / (float)N;   // exact: N is a power of two, so j * kInvN == j / N
+    const HairView& h = fg.h;
+    const int F = h.F;
+    const float* __restrict__ sdf = fg.sdf;
+    const float4* __restrict__ sdf8 = fg.sdf8;
+    const SdfGrid& sg = fg.sg;
+    const float margin = fg.margin, tip = fg.tip;
+    const int s = e / N, j = e % N;
+    const int gs = fg.firstStrand + s * (F + 1);
+    const size_t vg = (size_t)gs * N + j;
+    const float4 gp = h.pos[vg];
+    const float4 tn = h.tan[vg];
+    const bool collide = sdf && j >= 2;
+    const float factor = tip * ((float)j * kInvN) + 1.0f;
+    for (int i0 = 0; i0 <= F; i0 += U) {
+        float3 pt[U];
+        float wU[U], dist[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + u;
+            pt[u] = xyz(gp);
+            wU[u] = gp.w;
+            if (i > 0 && i <= F) {
+                const float4 off = __ldg(h.followOffset + gs + i);
+                pt[u] = add(xyz(gp), mul(factor, xyz(off)));
+                // inverse mass of the follow vertex: only this thread writes the word, after this read
+                wU[u] = __ldg(&h.pos[vg + (size_t)i * N].w);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            dist[u] = 1e10f;
+            if (collide && i0 + u <= F) dist[u] = sdf8 ? sdf_lookup8(sdf8, sg, pt[u]) : sdf_lookup(sdf, sg, pt[u]);
+        }
+        // vertices beyond the margin are final; the few within it run the gradient part in one loop
+        // (one copy of that code, not U)
+        unsigned near = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + u;
+            if (i > F) continue;
+            if (collide && dist[u] <= margin) {
+                near |= 1u << u;
+                continue;
+            }
+            if (i > 0) {
+                h.pos[vg + (size_t)i * N] = make_float4(pt[u].x, pt[u].y, pt[u].z, wU[u]);
+                h.tan[vg + (size_t)i * N] = tn;
+            }
+        }
+        while (near) {
+            const int u = __ffs(near) - 1;
+            near &= near - 1;
+            const int i = i0 + u;
+            const float3 p = u == 0 ? pt[0] : (u == 1 ? pt[1] : (u == 2 ? pt[2] : pt[3]));
+            const float d = u == 0 ? dist[0] : (u == 1 ? dist[1] : (u == 2 ? dist[2] : dist[3]));
+            const float w = u == 0 ? wU[0] : (u == 1 ? wU[1] : (u == 2 ? wU[2] : wU[3]));
+            const size_t v = vg + (size_t)i * N;
+            float3 proj = p;
+            const bool hit = collide_near(sdf, sdf8, sg, margin, p, d, &proj);
+            if (i > 0) {
+                h.pos[v] = make_float4(hit ? proj.x : p.x, hit ? proj.y : p.y, hit ? proj.z : p.z, w);
+                h.tan[v] = tn;
+            } else if (hit) {
+                h.pos[v] = with_xyz(gp, proj);
+            }
+            if (hit) h.prev[v] = with_xyz(h.prev[v], proj);
+        }
+    }
+}
+
 // ============================================================================================
 // follow hairs + collision
 //
@@ -613,71 +721,25 @@ __device__ __forceinline__ bool sdf_collide_from8(const float4* __restrict__ sdf
 // k_fused_strands has written the guides' constrained state and the frame's SDFs are built.  One
 // thread per guide vertex; it makes the vertex's F follow vertices (hair i = 1..F) from the guide's
 // pre-collision position, then collides the guide vertex and every follow vertex.  The loads of U
-// hairs are issued before any of them is collided or written, so their latencies overlap.
+// hairs are issued before any of them is collided or written, so their latencies overlap.  Each group
+// is cut into chunksPerItem chunks of guide vertices (a multiple of 256), which persistent blocks take
+// in turn: with few groups per block, smaller chunks spread groups of unequal cost (collisions) evenly
+// over the SMs; with many, whole groups keep the per-chunk overhead low.
 template <int N>
-__global__ void __launch_bounds__(256) k_follow_collide(const BatchObject* __restrict__ objs,
-                                                        const WorkItem* __restrict__ items, int numItems) {
-    constexpr int U = 4;
-    constexpr float kInvN = 1.0f / (float)N;   // exact: N is a power of two, so j * kInvN == j / N
-    for (int it = blockIdx.x; it < numItems; it += gridDim.x) {
+__global__ void __launch_bounds__(256, 3) k_follow_collide(const BatchObject* __restrict__ objs,
+                                                           const WorkItem* __restrict__ items, int numItems,
+                                                           int chunksPerItem) {
+    constexpr int kGroupVerts = fused_group_strands(N) * N;
+    const int chunkLen = ((kGroupVerts + chunksPerItem - 1) / chunksPerItem + 255) & ~255;
+    const int numChunks = numItems * chunksPerItem;
+    for (int c = blockIdx.x; c < numChunks; c += gridDim.x) {
+        const int it = c / chunksPerItem;
         const WorkItem wi = items[it];
-        const BatchObject& ob = objs[wi.obj];
-        const HairView h = ob.hair;
-        const int F = h.F;
-        const float* __restrict__ sdf = ob.sdf;
-        const float4* __restrict__ sdf8 = ob.sdf8;
-        if (F == 0 && !sdf) continue;
-        SdfGrid sg = SdfGrid{0.f, 0.f, 0.f, 1.f, 0, 0, 0, 0};
-        float margin = 0.0f;
-        if (sdf) { sg = ob.sdfFrame->grid; margin = ob.sdfFrame->margin; }
-        const float tip = ob.consts->tipSeparation;
-        const int gs0 = wi.firstGuide * (F + 1);
-        for (int e = threadIdx.x; e < wi.count * N; e += blockDim.x) {
-            const int s = e / N, j = e % N;
-            const int gs = gs0 + s * (F + 1);
-            const size_t vg = (size_t)gs * N + j;
-            const float4 gp = h.pos[vg];
-            const float4 tn = h.tan[vg];
-            const bool collide = sdf && j >= 2;
-            const float factor = tip * ((float)j * kInvN) + 1.0f;
-            for (int i0 = 0; i0 <= F; i0 += U) {
-                float3 pt[U];
-                float wU[U], dist[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int i = i0 + u;
-                    pt[u] = xyz(gp);
-                    wU[u] = gp.w;
-                    if (i > 0 && i <= F) {
-                        const float4 off = __ldg(h.followOffset + gs + i);
-                        pt[u] = add(xyz(gp), mul(factor, xyz(off)));
-                        // inverse mass of the follow vertex: only this thread writes the word, after this read
-                        wU[u] = __ldg(&h.pos[vg + (size_t)i * N].w);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    dist[u] = 1e10f;
-                    if (collide && i0 + u <= F) dist[u] = sdf8 ? sdf_lookup8(sdf8, sg, pt[u]) : sdf_lookup(sdf, sg, pt[u]);
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int i = i0 + u;
-                    if (i > F) continue;
-                    const size_t v = vg + (size_t)i * N;
-                    float3 proj = pt[u];
-                    const bool hit = collide && (sdf8 ? sdf_collide_from8(sdf8, sg, margin, pt[u], dist[u], proj)
-                                                      : sdf_collide_from(sdf, sg, margin, pt[u], dist[u], proj));
-                    if (i > 0) {
-                        h.pos[v] = make_float4(hit ? proj.x : pt[u].x, hit ? proj.y : pt[u].y, hit ? proj.z : pt[u].z, wU[u]);
-                        h.tan[v] = tn;
-                    } else if (hit) {
-                        h.pos[v] = with_xyz(gp, proj);
-                    }
-                    if (hit) h.prev[v] = with_xyz(h.prev[v], proj);
-                }
-            }
-        }
+        const int begin = (c - it * chunksPerItem) * chunkLen;
+        const int end = min(begin + chunkLen, wi.count * N);
+        FollowGroup fg;
+        if (!follow_group(objs[wi.obj], wi, fg)) continue;
+        for (int e = begin + (int)threadIdx.x; e < end; e += blockDim.x) follow_collide_vertex<N>(fg, e);
     }
 }
 
@@ -751,9 +813,11 @@ int fused_blocks_per_sm(int n, int vpl, int warps) {
     return 0;
 }
 
+int follow_max_chunks_per_item(int n) { return (fused_group_strands(n) * n + 255) / 256; }
+
 template <int N>
 static cudaError_t launch_follow_n(const FollowLaunch& fl, cudaStream_t s) {
-    k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems);
+    k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
     return cudaGetLastError();
 }
 

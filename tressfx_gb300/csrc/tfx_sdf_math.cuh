@@ -14,6 +14,19 @@ __device__ __forceinline__ uint32_t float_flip3(float f) {
 }
 __device__ __forceinline__ uint32_t ifloat_flip3(uint32_t u) { return (u >> 1) | (u << 31); }
 
+// True when p certainly fails the lookup's bounds test 0 <= ftoi((p - origin) / cell) < dims - 2 on
+// some axis, decided without the division.  d = p - origin is the reference's own first operation;
+// d <= -2 cell (exact product) gives a quotient <= -2, and d >= RN(dims * cell) >= dims * cell *
+// (1 - 2^-24) gives a quotient that truncates to dims - 1 or more (division is monotonic, dims is far
+// below 2^22).  Infinite d goes the same way as the reference (its quotient saturates); NaN and the
+// points near the range's faces take the exact path.
+__device__ __forceinline__ bool sdf_surely_outside(const SdfGrid& g, float3 p) {
+    const float dx = p.x - g.ox, dy = p.y - g.oy, dz = p.z - g.oz;
+    const float lo = -2.0f * g.cell;
+    return dx <= lo || dy <= lo || dz <= lo || dx >= (float)g.nx * g.cell || dy >= (float)g.ny * g.cell ||
+           dz >= (float)g.nz * g.cell;
+}
+
 // GetSdfCoordinates, :103-113
 __device__ __forceinline__ int3 sdf_coords(const SdfGrid& g, float3 p) {
     const float sx = (p.x - g.ox) / g.cell, sy = (p.y - g.oy) / g.cell, sz = (p.z - g.oz) / g.cell;
@@ -144,6 +157,7 @@ __device__ __forceinline__ void tri_cell_box(const SdfGrid& g, float3 t0, float3
 __device__ __forceinline__ float lerp_ref(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 
 __device__ __forceinline__ float sdf_lookup(const float* __restrict__ sdf, const SdfGrid& g, float3 p) {
+    if (sdf_surely_outside(g, p)) return 1e10f;
     const int3 gc = sdf_coords(g, p);
     if (!(0 <= gc.x && gc.x < g.nx - 2) || !(0 <= gc.y && gc.y < g.ny - 2) || !(0 <= gc.z && gc.z < g.nz - 2))
         return 1e10f;
