@@ -356,6 +356,15 @@ typedef enum tfx_batch_option {
     TFX_BATCH_OVERLAP_SDF = 2,      /* 1: the SDF build runs concurrently with the strand kernels    */
     TFX_BATCH_SDF_BLOCK = 3         /* threads per block of the SDF construct: 64, 128 or 256         */
 } tfx_batch_option;
+/* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
+ * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (float4 per
+ * vertex; pinned memory copies fastest).  The call queues a device snapshot on the context's stream
+ * and its copy to the host on a separate copy stream, so the copy overlaps the next frames; it
+ * returns at once with a ticket.  The destination must stay valid and untouched until
+ * tfx_batch_wait_readback(ticket) returns.  No counterpart in the reference (its renderer reads the
+ * buffers on the GPU); this is how a host consumer takes frames without stalling the simulation. */
+int tfx_batch_readback(tfx_batch batch, void* const* host_dst, int count, int64_t* ticket);
+int tfx_batch_wait_readback(tfx_batch batch, int64_t ticket);
 int tfx_batch_set_option(tfx_batch batch, int option, int value);
 int tfx_batch_get_option(tfx_batch batch, int option, int* value);
 /* Per-frame inputs (copied when tfx_batch_run is called): the constant block of hair object

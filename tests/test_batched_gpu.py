@@ -176,3 +176,35 @@ def test_batched_follow_collide_many_contacts_bit_exact(ctx, follows):
         assert_same(gpu.hair[0], ora.hair[0], f"follows={follows}")
     finally:
         gpu.close()
+
+
+@pytest.mark.gpu
+def test_batched_readback_delivers_each_frame(ctx):
+    """tfx_batch_readback: the positions after each frame reach host memory bit for bit while later
+    frames run; bad tickets and destination counts are refused."""
+    from tressfx_gb300.api import PinnedArray
+    sc = scene_head(seed=31, num_guides=200, n=16, follows=2, triangles=2500, sdf_cells=40, frames=6)
+    gpu = BatchedPipeline(ctx, sc)
+    bufs = [[PinnedArray((h.num_vertices, 4), np.float32) for h in gpu.hair] for _ in range(3)]
+    try:
+        tickets, want = [], []
+        for f in range(6):
+            gpu.step(f)
+            tickets.append(gpu.batch.readback([b.array.ctypes.data for b in bufs[f % 3]]))
+            if f >= 2:
+                gpu.batch.wait_readback(tickets[f - 2])
+                assert np.array_equal(bufs[(f - 2) % 3][0].array.view(np.uint32), want[f - 2].view(np.uint32)), f
+            ctx.synchronize()
+            want.append(gpu.hair[0].read(A.BUF_POSITIONS).copy())
+        for f in (4, 5):
+            gpu.batch.wait_readback(tickets[f])
+            assert np.array_equal(bufs[f % 3][0].array.view(np.uint32), want[f].view(np.uint32)), f
+        with pytest.raises(Exception):
+            gpu.batch.wait_readback(99)
+        with pytest.raises(Exception):
+            gpu.batch.readback([])
+    finally:
+        for side in bufs:
+            for b in side:
+                b.free()
+        gpu.close()

@@ -432,6 +432,16 @@ class Batch:
     def run(self) -> None:
         check(A.lib().tfx_batch_run(self.handle), "tfx_batch_run")
 
+    def readback(self, host_ptrs: list[int]) -> int:
+        """Queues the copy of every hair object's positions into host memory; returns a ticket."""
+        arr = (C.c_void_p * len(host_ptrs))(*host_ptrs)
+        tk = C.c_int64()
+        check(A.lib().tfx_batch_readback(self.handle, arr, len(host_ptrs), C.byref(tk)), "tfx_batch_readback")
+        return tk.value
+
+    def wait_readback(self, ticket: int) -> None:
+        check(A.lib().tfx_batch_wait_readback(self.handle, int(ticket)), "tfx_batch_wait_readback")
+
     def profile_frame(self) -> list[float]:
         ms = (C.c_float * 16)()
         n = C.c_int()

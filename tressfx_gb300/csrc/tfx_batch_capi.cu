@@ -82,6 +82,16 @@ struct tfx_batch_t {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int launchesPerFrame = 0;
     std::string description;
+
+    // tfx_batch_readback: two device snapshots of every object's positions, copied to the host on
+    // `copy` while the next frames run
+    cudaStream_t copy = nullptr;
+    char* snap[2] = {nullptr, nullptr};
+    std::vector<size_t> snapOff;     // per hair object: offset in a snapshot
+    size_t snapBytes = 0;
+    cudaEvent_t snapDone[2] = {nullptr, nullptr}, copyDone[2] = {nullptr, nullptr};
+    bool copyUsed[2] = {false, false};
+    int64_t nextTicket = 0;
 };
 
 static int batch_fail_built(const char* who) { return fail(TFX_ERR_INVALID_ARGUMENT, "%s: the batch is already built", who); }
@@ -105,6 +115,13 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
         if (b->pinned[i]) cudaFreeHost(b->pinned[i]);
         if (b->done[i]) cudaEventDestroy(b->done[i]);
     }
+    if (b->copy) cudaStreamSynchronize(b->copy);
+    for (int i = 0; i < 2; ++i) {
+        if (b->snap[i]) cudaFree(b->snap[i]);
+        if (b->snapDone[i]) cudaEventDestroy(b->snapDone[i]);
+        if (b->copyDone[i]) cudaEventDestroy(b->copyDone[i]);
+    }
+    if (b->copy) cudaStreamDestroy(b->copy);
     if (b->pinnedErr) cudaFreeHost(b->pinnedErr);
     if (b->evFork) cudaEventDestroy(b->evFork);
     if (b->evJoin) cudaEventDestroy(b->evJoin);
@@ -714,6 +731,67 @@ extern "C" int tfx_batch_run(tfx_batch b) {
     TFX_CUDA(cudaGraphLaunch(b->graph[s], b->ctx->stream), "cudaGraphLaunch");
     TFX_CUDA(cudaEventRecord(b->done[s], b->ctx->stream), "cudaEventRecord");
     b->used[s] = true;
+    return TFX_OK;
+}
+
+static int readback_init(tfx_batch b) {
+    if (b->copy) return TFX_OK;
+    b->snapOff.assign(b->hairs.size(), 0);
+    size_t off = 0;
+    for (size_t i = 0; i < b->hairs.size(); ++i) {
+        b->snapOff[i] = off;
+        off += ((size_t)b->hairs[i]->Vtot * sizeof(float4) + 255) & ~(size_t)255;
+    }
+    b->snapBytes = off;
+    for (int i = 0; i < 2; ++i) {
+        TFX_CUDA(cudaMalloc(&b->snap[i], std::max<size_t>(off, 256)), "tfx_batch_readback: snapshot buffer");
+        TFX_CUDA(cudaEventCreateWithFlags(&b->snapDone[i], cudaEventDisableTiming), "cudaEventCreate");
+        TFX_CUDA(cudaEventCreateWithFlags(&b->copyDone[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    TFX_CUDA(cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking), "tfx_batch_readback: copy stream");
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_readback(tfx_batch b, void* const* host_dst, int count, int64_t* ticket) {
+    if (!b || !host_dst || !ticket) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: null argument");
+    if (!b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: batch not built");
+    if (count != (int)b->hairs.size())
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: %d destinations for %d hair objects", count,
+                    (int)b->hairs.size());
+    for (int i = 0; i < count; ++i)
+        if (!host_dst[i]) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: destination %d is null", i);
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    if (int r = readback_init(b)) return r;
+    const int64_t t = b->nextTicket;
+    const int s = (int)(t & 1);
+    cudaStream_t main = b->ctx->stream;
+    // the snapshot may not overwrite a buffer whose copy to the host is still running
+    if (b->copyUsed[s]) TFX_CUDA(cudaStreamWaitEvent(main, b->copyDone[s], 0), "cudaStreamWaitEvent");
+    for (int i = 0; i < count; ++i) {
+        tfx_hair h = b->hairs[i];
+        TFX_CUDA(cudaMemcpyAsync(b->snap[s] + b->snapOff[i], h->view.pos, (size_t)h->Vtot * sizeof(float4),
+                                 cudaMemcpyDeviceToDevice, main), "tfx_batch_readback: snapshot");
+    }
+    TFX_CUDA(cudaEventRecord(b->snapDone[s], main), "cudaEventRecord");
+    TFX_CUDA(cudaStreamWaitEvent(b->copy, b->snapDone[s], 0), "cudaStreamWaitEvent");
+    for (int i = 0; i < count; ++i) {
+        tfx_hair h = b->hairs[i];
+        TFX_CUDA(cudaMemcpyAsync(host_dst[i], b->snap[s] + b->snapOff[i], (size_t)h->Vtot * sizeof(float4),
+                                 cudaMemcpyDeviceToHost, b->copy), "tfx_batch_readback: copy to host");
+    }
+    TFX_CUDA(cudaEventRecord(b->copyDone[s], b->copy), "cudaEventRecord");
+    b->copyUsed[s] = true;
+    b->nextTicket = t + 1;
+    *ticket = t;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_wait_readback(tfx_batch b, int64_t ticket) {
+    if (!b || ticket < 0 || ticket >= b->nextTicket)
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_wait_readback: no readback %lld", (long long)ticket);
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    // the copy stream runs in order: the slot's latest copy finishing implies this one finished
+    TFX_CUDA(cudaEventSynchronize(b->copyDone[ticket & 1]), "tfx_batch_wait_readback");
     return TFX_OK;
 }
 
