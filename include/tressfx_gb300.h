@@ -427,7 +427,10 @@ int tfx_nsdf_evaluate(tfx_nsdf nsdf, int pool, float* pred_cells, float* target_
 int tfx_nsdf_query(tfx_nsdf nsdf, const void* points, int count, const float pose[3], float* out);
 /* CollideHairVerticesWithSdf_forward for every vertex of `hair` with the proxy in front of the grid:
  * the band vertices are collided on `sdf` (mesh already bound and skinned for this frame), built on
- * `grid` at their cells only.  band_count (optional, host) receives the band size and synchronizes. */
+ * `grid` at their cells only.  A pose outside the range of the training poses (pool 0) takes the
+ * grid path for every vertex: the whole grid is built (tfx_sdf_update) and collided
+ * (tfx_sdf_collide), and band_count reports every vertex.  band_count (optional, host) receives the
+ * band size and synchronizes. */
 int tfx_nsdf_collide(tfx_nsdf nsdf, tfx_hair hair, tfx_sdf sdf, const tfx_sdf_grid* grid, float margin_world,
                      const float pose[3], int32_t* band_count);
 /* Master FP32 parameters (tfx_nsdf_get_info's num_params floats), e.g. to save or load a network. */

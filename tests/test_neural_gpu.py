@@ -89,3 +89,29 @@ def test_collision_through_the_proxy_matches_the_grid(ctx, small_proxy):
     finally:
         a.close()
         b.close()
+
+
+def test_pose_outside_training_range_takes_the_grid_path(ctx, small_proxy):
+    """A pose outside the range the proxy was trained on: every vertex is collided on the full grid,
+    so the frames equal the grid-collided ones bit for bit and the band reports every vertex."""
+    from tressfx_gb300 import _capi as A
+    from tressfx_gb300.headless import FrameInputs, NeuralPipeline, PlainPipeline
+    sc, nsdf, _ = small_proxy
+    pose_fn = sc.meta["pose_fn"]
+    sc.meta["pose_fn"] = lambda t: (2.5, -2.5, 2.5)   # radians, far outside the +-40 degree training poses
+    a = PlainPipeline(ctx, sc)
+    b = NeuralPipeline(ctx, sc, nsdf)
+    try:
+        for f in range(6):
+            a.step(f)
+            fin = FrameInputs(sc, f)
+            b.prepare(fin)
+            b.run(fin, record_band=True)
+        assert b.band_counts[-1] == b.hair[0].num_vertices
+        for buf in (A.BUF_POSITIONS, A.BUF_POSITIONS_PREV, A.BUF_TANGENTS):
+            x, y = a.hair[0].read(buf).view(np.uint32), b.hair[0].read(buf).view(np.uint32)
+            assert np.array_equal(x, y), f"buffer {buf}"
+    finally:
+        sc.meta["pose_fn"] = pose_fn
+        a.close()
+        b.close()

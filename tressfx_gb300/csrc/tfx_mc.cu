@@ -9,10 +9,10 @@
 //   k_mc_count: one cell per thread, the vertex count every block of 256 cells reserves;
 //   k_mc_scan:  one block, the exclusive prefix of those counts (64-bit) and the total (the shader's
 //               counter, which also counts cubes that did not fit);
-//   k_mc_write: each block rescans its cells in shared memory and spreads its output vertices over its
-//               threads, one 32-byte vertex per thread (coalesced stores); a cube is written only if
-//               its range ends below max_vertices (the shader's `offset + num < max`), and whatever
-//               InitializeMCVertices would leave zero is zeroed.
+//   k_mc_write: each block rescans its cells in shared memory and spreads its triangles over its
+//               threads, one triangle per thread; a cube is written only if its range ends below
+//               max_vertices (the shader's `offset + num < max`), and whatever InitializeMCVertices
+//               would leave zero is zeroed.
 // The grid (a few MB) stays in L2 between the passes.
 #include <cstring>
 #include <new>
@@ -43,12 +43,37 @@ __constant__ int8_t kCornerZ[8] = {0, 0, 1, 1, 0, 0, 1, 1};
 __constant__ int8_t kEdgeA[12] = {0, 1, 2, 3, 4, 5, 6, 7, 0, 1, 2, 3};
 __constant__ int8_t kEdgeB[12] = {1, 2, 3, 0, 5, 6, 7, 4, 4, 5, 6, 7};
 
+// Division of 32-bit unsigned n by an invariant d >= 1 with a multiply-high (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994, figure 4.1):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, q = (umulhi(n, m) + n) >> l, the sum taken in
+// 64 bits.  Exact for every n < 2^32.
+struct FastDiv {
+    uint32_t d, m, l;
+};
+
+__host__ FastDiv fast_div(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 32 && (1ull << l) < d) ++l;
+    const uint64_t m = (((1ull << l) - d) << 32) / d + 1;
+    return FastDiv{d, (uint32_t)m, l};
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return (uint32_t)(((uint64_t)__umulhi(n, f.m) + n) >> f.l);
+}
+
+// The grid's two divisors: cells per line (X) and per plane (X * Y).
+struct McDims {
+    FastDiv line, plane;
+};
+
 // The cell of linear index `index` (x fastest), as GetSdfCellPositionFromIndex computes it.
-__device__ __forceinline__ int3 mc_cell_xyz(const SdfGrid& g, int index) {
-    const uint32_t perLine = (uint32_t)g.nx, perPlane = (uint32_t)(g.nx * g.ny);
+__device__ __forceinline__ int3 mc_cell_xyz(const McDims& dm, int index) {
     const uint32_t u = (uint32_t)index;
-    const uint32_t rem = u % perPlane;
-    return make_int3((int)(rem % perLine), (int)(rem / perLine), (int)(u / perPlane));
+    const uint32_t z = fdiv(u, dm.plane);
+    const uint32_t rem = u - z * dm.plane.d;
+    const uint32_t y = fdiv(rem, dm.line);
+    return make_int3((int)(rem - y * dm.line.d), (int)y, (int)z);
 }
 
 // The eight corner values of cube `c` and its cubeIndex; -1 for cells on the upper faces of the grid.
@@ -113,8 +138,8 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* red, T* total) {
 }
 
 // Pass 1: the vertices every block of 256 cells reserves.
-__global__ void __launch_bounds__(kMcThreads) k_mc_count(const float* __restrict__ sdf, SdfGrid g, float iso,
-                                                         const McTables* __restrict__ T, int totalCells,
+__global__ void __launch_bounds__(kMcThreads) k_mc_count(const float* __restrict__ sdf, SdfGrid g, McDims dm,
+                                                         float iso, const McTables* __restrict__ T, int totalCells,
                                                          int* __restrict__ blockSums) {
     __shared__ int cnt[256];
     __shared__ int red[kMcThreads / 32];
@@ -124,7 +149,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_count(const float* __restrict
     int nv = 0;
     if (idx < totalCells) {
         float s[8];
-        const int cfg = mc_config(sdf, g, mc_cell_xyz(g, idx), iso, s);
+        const int cfg = mc_config(sdf, g, mc_cell_xyz(dm, idx), iso, s);
         nv = cfg >= 0 ? cnt[cfg] : 0;
     }
 #pragma unroll
@@ -140,17 +165,29 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_count(const float* __restrict
 }
 
 // Pass 2 (one block): exclusive prefix of the block sums in 64 bits; blockOff[nb] = the total, and
-// the counter (an int, as in the shader) its low 32 bits.
+// the counter (an int, as in the shader) its low 32 bits.  Each thread takes 8 consecutive sums of a
+// 8192-sum tile (all loads in flight at once), scans them serially, and the block scans the thread
+// totals.
+constexpr int kMcScanPer = 8;
 __global__ void __launch_bounds__(kMcScanThreads) k_mc_scan(const int* __restrict__ blockSums, int nb,
                                                             long long* __restrict__ blockOff, int* __restrict__ counter) {
     __shared__ long long red[kMcScanThreads / 32];
     long long carry = 0;
-    for (int base = 0; base < nb; base += kMcScanThreads) {
-        const int b = base + (int)threadIdx.x;
-        const long long v = b < nb ? blockSums[b] : 0;
+    for (int base = 0; base < nb; base += kMcScanThreads * kMcScanPer) {
+        const int b0 = base + (int)threadIdx.x * kMcScanPer;
+        int v[kMcScanPer];
+#pragma unroll
+        for (int k = 0; k < kMcScanPer; ++k) v[k] = b0 + k < nb ? __ldg(blockSums + b0 + k) : 0;
+        long long mine = 0;
+#pragma unroll
+        for (int k = 0; k < kMcScanPer; ++k) mine += v[k];
         long long total;
-        const long long ex = block_exclusive_scan<kMcScanThreads>(v, red, &total);
-        if (b < nb) blockOff[b] = carry + ex;
+        long long run = carry + block_exclusive_scan<kMcScanThreads>(mine, red, &total);
+#pragma unroll
+        for (int k = 0; k < kMcScanPer; ++k) {
+            if (b0 + k < nb) blockOff[b0 + k] = run;
+            run += v[k];
+        }
         carry += total;
     }
     if (threadIdx.x == 0) {
@@ -164,19 +201,19 @@ __device__ __forceinline__ void mc_zero(float4* out, long long v) {
     out[2 * v + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// Pass 3: the block's cells are scanned in shared memory, then its output vertices are spread over
-// the threads (thread k writes vertex k, 32 contiguous bytes: coalesced); each thread evaluates the
-// three edge vertices and the normal of its vertex's triangle.  A cube that does not end below
-// maxVerts gets zeros in its range (below maxVerts), and so do the vertices past a count that is not
-// a multiple of 3.  Vertices [total, maxVerts) are zeroed by all blocks together.
-__global__ void __launch_bounds__(kMcThreads) k_mc_write(const float* __restrict__ sdf, SdfGrid g, float iso,
-                                                         const McTables* __restrict__ T, int totalCells,
+// Pass 3: the block's cells are scanned in shared memory (vertex and triangle counts packed in one
+// int), each cell's thread zeroes what of its range will not be written (a cube that does not end
+// below maxVerts, or the vertices past a count that is not a multiple of 3), then the block's
+// triangles are spread over its threads, one triangle (three 32-byte vertices) per thread.  Vertices
+// [total, maxVerts) are zeroed by all blocks together.
+__global__ void __launch_bounds__(kMcThreads) k_mc_write(const float* __restrict__ sdf, SdfGrid g, McDims dm,
+                                                         float iso, const McTables* __restrict__ T, int totalCells,
                                                          const int* __restrict__ blockSums,
                                                          const long long* __restrict__ blockOff, int nb, int maxVerts,
                                                          float4* __restrict__ out) {
     __shared__ float cs[8 * kMcThreads];      // corner values, [corner][cell]
-    __shared__ int ccfg[kMcThreads];
-    __shared__ int cstart[kMcThreads + 1];
+    __shared__ int ccfg[kMcThreads];          // cubeIndex of a cube whose triangles are written, else -1
+    __shared__ int cex[kMcThreads + 1];       // exclusive prefix: vertices in the low 16 bits, triangles above
     __shared__ int red[kMcThreads / 32];
     const long long total = __ldg(blockOff + nb);
     for (long long v = total + (long long)blockIdx.x * kMcThreads + threadIdx.x; v < maxVerts;
@@ -190,51 +227,56 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_write(const float* __restrict
     int nv = 0, cfg = -1;
     if (idx < totalCells) {
         float s[8];
-        cfg = mc_config(sdf, g, mc_cell_xyz(g, idx), iso, s);
+        cfg = mc_config(sdf, g, mc_cell_xyz(dm, idx), iso, s);
         if (cfg >= 0) {
             nv = __ldg(T->count + cfg);
 #pragma unroll
             for (int k = 0; k < 8; ++k) cs[k * kMcThreads + threadIdx.x] = s[k];
         }
     }
-    ccfg[threadIdx.x] = cfg;
+    const int ntri = nv / 3;
     int sum;
-    const int ex = block_exclusive_scan<kMcThreads>(nv, red, &sum);
-    cstart[threadIdx.x] = ex;
-    if (threadIdx.x == 0) cstart[kMcThreads] = sum;
+    const int ex = block_exclusive_scan<kMcThreads>(nv | (ntri << 16), red, &sum);
+    cex[threadIdx.x] = ex;
+    if (threadIdx.x == 0) cex[kMcThreads] = sum;
+    const long long cellOff = off + (ex & 0xffff);
+    const bool fits = nv > 0 && cellOff + nv < maxVerts;
+    ccfg[threadIdx.x] = fits ? cfg : -1;
+    if (nv > 0) {
+        for (int k = fits ? 3 * ntri : 0; k < nv && cellOff + k < maxVerts; ++k) mc_zero(out, cellOff + k);
+    }
     __syncthreads();
-    for (int k = threadIdx.x; k < mine; k += kMcThreads) {
-        const long long v = off + k;
-        if (v >= maxVerts) break;
-        // the cube holding vertex k: the last c with cstart[c] <= k (counts of 0 repeat a start)
+    const int mineT = sum >> 16;
+    for (int k = threadIdx.x; k < mineT; k += kMcThreads) {
+        // the cube holding triangle k: the last c with a triangle prefix <= k
         int lo = 0, hi = kMcThreads - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (cstart[mid] <= k) lo = mid; else hi = mid - 1;
+            if ((cex[mid] >> 16) <= k) lo = mid; else hi = mid - 1;
         }
         const int c = lo;
-        const int r = k - cstart[c];
-        const int n = cstart[c + 1] - cstart[c];
-        if (!(off + cstart[c] + n < maxVerts) || r >= 3 * (n / 3)) {
-            mc_zero(out, v);
-            continue;
-        }
         const int cf = ccfg[c];
-        const int3 xyz = mc_cell_xyz(g, cell0 + c);
-        const int* tri = T->tri + 16 * cf + 3 * (r / 3);
-        const float* s = cs + c;
-        const float3 v0 = mc_edge_vertex(xyz, g, s, __ldg(tri), iso);
-        const float3 v1 = mc_edge_vertex(xyz, g, s, __ldg(tri + 1), iso);
-        const float3 v2 = mc_edge_vertex(xyz, g, s, __ldg(tri + 2), iso);
+        if (cf < 0) continue;
+        const int t = k - (cex[c] >> 16);
+        const int3 xyz = mc_cell_xyz(dm, cell0 + c);
+        const int* tri = T->tri + 16 * cf + 3 * t;
+        const float* cv = cs + c;
+        const float3 v0 = mc_edge_vertex(xyz, g, cv, __ldg(tri), iso);
+        const float3 v1 = mc_edge_vertex(xyz, g, cv, __ldg(tri + 1), iso);
+        const float3 v2 = mc_edge_vertex(xyz, g, cv, __ldg(tri + 2), iso);
         // normalize(cross(v1 - v0, v2 - v0)) = n * (1 / sqrt(dot(n, n)))
         const float3 a = make_float3(v1.x - v0.x, v1.y - v0.y, v1.z - v0.z);
         const float3 b = make_float3(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z);
         const float3 nn = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
         const float inv = 1.0f / sqrtf(nn.x * nn.x + nn.y * nn.y + nn.z * nn.z);
-        const int corner = r % 3;
-        const float3 pv = corner == 0 ? v0 : (corner == 1 ? v1 : v2);
-        out[2 * v] = make_float4(pv.x, pv.y, pv.z, 0.f);
-        out[2 * v + 1] = make_float4(nn.x * inv, nn.y * inv, nn.z * inv, 0.f);
+        const float4 n4 = make_float4(nn.x * inv, nn.y * inv, nn.z * inv, 0.f);
+        float4* o = out + 2 * (off + (cex[c] & 0xffff) + 3 * t);
+        o[0] = make_float4(v0.x, v0.y, v0.z, 0.f);
+        o[1] = n4;
+        o[2] = make_float4(v1.x, v1.y, v1.z, 0.f);
+        o[3] = n4;
+        o[4] = make_float4(v2.x, v2.y, v2.z, 0.f);
+        o[5] = n4;
     }
 }
 
@@ -252,9 +294,10 @@ cudaError_t launch_marching_cubes(const float* sdf, const SdfGrid& g, float iso,
     const int nb = mc_num_blocks(cells);
     int* blockSums = (int*)scratch;
     long long* blockOff = (long long*)((char*)scratch + (((size_t)nb * sizeof(int) + 15) & ~(size_t)15));
-    k_mc_count<<<nb, kMcThreads, 0, s>>>(sdf, g, iso, tables, (int)cells, blockSums);
+    const McDims dm{fast_div((uint32_t)g.nx), fast_div((uint32_t)g.nx * (uint32_t)g.ny)};
+    k_mc_count<<<nb, kMcThreads, 0, s>>>(sdf, g, dm, iso, tables, (int)cells, blockSums);
     k_mc_scan<<<1, kMcScanThreads, 0, s>>>(blockSums, nb, blockOff, counter);
-    k_mc_write<<<nb, kMcThreads, 0, s>>>(sdf, g, iso, tables, (int)cells, blockSums, blockOff, nb, maxVerts, out);
+    k_mc_write<<<nb, kMcThreads, 0, s>>>(sdf, g, dm, iso, tables, (int)cells, blockSums, blockOff, nb, maxVerts, out);
     return cudaGetLastError();
 }
 

@@ -1,5 +1,7 @@
 // C ABI of the learned collision proxy (tfx_nsdf_*): training data from the method's own grid SDFs,
 // training, evaluation against the grids, queries, and collision with the exact-grid fallback.
+#include <algorithm>
+#include <climits>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -34,6 +36,8 @@ struct tfx_nsdf_t {
     uint32_t* marks = nullptr;
     int64_t marksCap = 0;           // words
     int* band_ = nullptr;           // [0] = count, then the list
+    float poseLo[3] = {1e30f, 1e30f, 1e30f};   // range of the training poses (pool 0)
+    float poseHi[3] = {-1e30f, -1e30f, -1e30f};
     int64_t bandCap = 0;
 };
 
@@ -146,6 +150,11 @@ extern "C" int tfx_nsdf_add_samples(tfx_nsdf h, int pool, tfx_mesh mesh, tfx_sdf
                                         h->ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "tfx_nsdf_add_samples: sample launch");
     h->poolSize[pool] += count;
+    if (pool == 0 && pose)
+        for (int k = 0; k < 3; ++k) {
+            h->poseLo[k] = std::min(h->poseLo[k], pose[k]);
+            h->poseHi[k] = std::max(h->poseHi[k], pose[k]);
+        }
     return TFX_OK;
 }
 
@@ -229,6 +238,18 @@ extern "C" int tfx_nsdf_collide(tfx_nsdf h, tfx_hair hair, tfx_sdf sdf, const tf
         return fail(TFX_ERR_SIZE, "tfx_nsdf_collide: grid of %lld cells (allocation %lld)", (long long)cells, (long long)sdf->alloc);
     if (sdf->ntri > 0 && !sdf->mesh) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_nsdf_collide: no collision mesh bound");
     TFX_CUDA(cudaSetDevice(h->ctx->device), "cudaSetDevice");
+    // a pose outside the range the network was trained on: the grid path for every vertex
+    bool inRange = pose != nullptr;
+    for (int k = 0; k < 3 && inRange; ++k) inRange = pose[k] >= h->poseLo[k] && pose[k] <= h->poseHi[k];
+    if (!inRange) {
+        if (int r = tfx_sdf_update(sdf, grid)) return r;
+        if (int r = tfx_sdf_collide(sdf, hair, grid, margin_world)) return r;
+        if (band_count) {
+            *band_count = (int32_t)std::min<int64_t>(hair->Vtot, INT32_MAX);
+            TFX_CUDA(cudaStreamSynchronize(h->ctx->stream), "cudaStreamSynchronize");
+        }
+        return TFX_OK;
+    }
     if (int r = nsdf_grow((void**)&h->marks, &h->marksCap, (cells + 31) / 32, sizeof(uint32_t), "tfx_nsdf_collide: marks")) return r;
     if (int r = nsdf_grow((void**)&h->band_, &h->bandCap, hair->Vtot + 1, sizeof(int), "tfx_nsdf_collide: band")) return r;
     nsdf::CollideArgs a{};
