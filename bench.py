@@ -52,6 +52,16 @@ WORKLOADS = {
 
 
 # ------------------------------------------------------------------------------------------ utils
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel, from
+# one ncu --set full capture of the same workload at frame 21 (the capture and its command are
+# summarised in profiles/k_fused_strands_k_follow_collide_head_n32.md).  ncu flushes the caches
+# before the capture and does not count writes still in L2 when the kernel ends.
+NCU_TRAFFIC = {
+    ("head", "k_follow_collide (n=32)"): 102.1e6,
+    ("head", "k_fused_strands (n=32)"): 47.6e6,
+}
+
+
 def load_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -653,7 +663,8 @@ def main() -> None:
                     "d2h_bytes_per_step": b["d2h"], "ms_per_step": b["e2e_ms_per_step"]},
             "gpu_launches": b["launches_per_frame"] * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved,
-                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": NCU_TRAFFIC.get((args.config, dom_name)),
                          "peak_source": peaks["source"], "algorithmic_bytes": dom_bytes, "launch_ms": dom_ms},
             "kernel_ms": kern,
             "kernel_gbs": gbs,
