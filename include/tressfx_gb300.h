@@ -354,7 +354,10 @@ typedef enum tfx_batch_option {
                                        per cell): 0 never, 1 always, 2 (default) for the SDFs whose
                                        objects make at least 4 lookups per cell each frame          */
     TFX_BATCH_OVERLAP_SDF = 2,      /* 1: the SDF build runs concurrently with the strand kernels    */
-    TFX_BATCH_SDF_BLOCK = 3         /* threads per block of the SDF construct: 64, 128 or 256         */
+    TFX_BATCH_SDF_BLOCK = 3,        /* threads per block of the SDF construct: 64, 128 or 256         */
+    TFX_BATCH_SPLIT_SWEEPS = 4      /* 1: the local-shape sweeps run as their own launch (a thread per
+                                       strand, up to four sweeps pipelined in registers) between two
+                                       passes of the strand kernel; 0: inside the strand kernel      */
 } tfx_batch_option;
 /* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
  * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (float4 per

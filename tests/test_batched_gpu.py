@@ -208,3 +208,25 @@ def test_batched_readback_delivers_each_frame(ctx):
             for b in side:
                 b.free()
         gpu.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,iters", [(4, 2), (16, 6), (32, 3), (64, 2)])
+@pytest.mark.parametrize("split", [0, 1])
+def test_batched_split_sweeps_bit_exact(ctx, n, iters, split):
+    """The local-shape sweeps inside the strand kernel (0) or as their own launch between its two
+    halves, up to four sweeps pipelined in a thread's registers and more in waves (1): the oracle's
+    buffers either way, for every strand length (n = 64 runs one sweep per frame, the reference rule)."""
+    sc = scene_head(seed=37, num_guides=150, n=n, follows=1, triangles=2500, sdf_cells=40, frames=4)
+    sc.objects[0].settings["local_constraints_iterations"] = iters
+    gpu = BatchedPipeline(ctx, sc)
+    try:
+        gpu.batch.set_option(gpu.batch.SPLIT_SWEEPS, split)
+        assert gpu.batch.get_option(gpu.batch.SPLIT_SWEEPS) == split
+        ora = OraclePipeline(sc)
+        for f in range(4):
+            fin = gpu.step(f)
+            ora.step(fin)
+        assert_same(gpu.hair[0], ora.hair[0], f"n={n} iters={iters} split={split}")
+    finally:
+        gpu.close()

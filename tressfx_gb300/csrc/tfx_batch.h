@@ -60,6 +60,7 @@ struct FusedLaunch {
     const WorkItem* items;
     int numItems;
     int* err;        // set to 1 when a block gives up waiting for its bulk copies
+    int mode;        // 0 the whole frame, 1 up to the local-shape sweeps, 2 after them
 };
 
 struct FollowLaunch {
@@ -80,6 +81,8 @@ struct SdfBatchLaunch {
 };
 
 cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s);
+// k_local_sweep over the groups of fl (mode 1 has run on them, mode 2 runs after)
+cudaError_t launch_local_sweep(const FusedLaunch& fl, cudaStream_t s);
 cudaError_t launch_follow_collide(const FollowLaunch& fl, cudaStream_t s);
 cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s);
 cudaError_t launch_batch_sdf(const SdfBatchLaunch& l, cudaStream_t s);

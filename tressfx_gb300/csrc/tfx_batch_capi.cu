@@ -34,6 +34,7 @@ struct BatchClass {
     int perSMCap = 0;            // resident strand blocks per SM allowed (0 = as many as fit)
     int followBlocks = 1;        // grid of k_follow_collide (persistent over the chunks)
     int followChunks = 1;        // chunks per group in k_follow_collide
+    bool splitSweeps = false;    // local-shape sweeps in k_local_sweep between two strand passes
     std::vector<WorkItem> hostItems;
     WorkItem* items = nullptr;  // device
     int numItems = 0;
@@ -184,8 +185,9 @@ static void describe(tfx_batch b) {
     char buf[1024];
     int k = snprintf(buf, sizeof(buf), "sdf construct %d threads/block;", b->sdfL.constructThreads);
     for (auto& c : b->classes)
-        k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d;",
-                      c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n));
+        k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d%s;",
+                      c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n),
+                      c.splitSweeps ? ", sweeps in their own launch" : "");
     k += snprintf(buf + k, sizeof(buf) - k, " SDF build %s the strand kernels%s;",
                   b->overlap ? "concurrent with" : "before", b->sdfL.expand ? ", lookups on corner-expanded grids" : "");
     b->description = buf;
@@ -238,8 +240,17 @@ static int launch_sdf_part(tfx_batch b, cudaStream_t s) {
 }
 
 static int launch_strands(tfx_batch b, BatchClass& c, cudaStream_t s) {
-    FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems, b->devErr};
-    cudaError_t e = launch_fused_strands(fl, s);
+    FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems, b->devErr, 0};
+    cudaError_t e;
+    if (!c.splitSweeps) {
+        e = launch_fused_strands(fl, s);
+    } else {   // the sweeps as their own launch, between the two halves of the strand kernel
+        fl.mode = 1;
+        e = launch_fused_strands(fl, s);
+        if (e == cudaSuccess) e = launch_local_sweep(fl, s);
+        fl.mode = 2;
+        if (e == cudaSuccess) e = launch_fused_strands(fl, s);
+    }
     return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: fused strand launch");
 }
 
@@ -338,7 +349,7 @@ static int capture_graphs(tfx_batch b) {
     }
     int launches = (b->totalMeshVerts > 0 ? 1 : 0) +
                    (b->sdfs.empty() ? 0 : (b->sdfL.totalTris > 0 ? 3 : 2) + (b->sdfL.expand ? 1 : 0));
-    for (auto& c : b->classes) launches += c.numItems > 0 ? 2 : 0;
+    for (auto& c : b->classes) launches += c.numItems > 0 ? (c.splitSweeps ? 4 : 2) : 0;
     b->launchesPerFrame = launches;
     return TFX_OK;
 }
@@ -463,6 +474,12 @@ static int autotune(tfx_batch b, int frames) {
         }
         c.vpl = bestV; c.warps = bestW; c.perSMCap = bestCap;
         if (rc == TFX_OK) rc = size_class(b, c);
+        if (rc == TFX_OK) {   // the sweeps in the strand kernel, or as their own launch
+            c.splitSweeps = !c.splitSweeps;
+            float ms;
+            if ((rc = time_graph_frames(b, frames, &ms)) == TFX_OK && !(ms < best)) c.splitSweeps = !c.splitSweeps;
+            else if (rc == TFX_OK) best = ms;
+        }
     }
     int rr = snapshot_restore(sn, s);
     return rc ? rc : rr;
@@ -832,6 +849,10 @@ extern "C" int tfx_batch_set_option(tfx_batch b, int option, int value) {
                 return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: SDF block %d (64, 128 or 256)", value);
             b->sdfL.constructThreads = value;
             break;
+        case TFX_BATCH_SPLIT_SWEEPS:
+            if (value != 0 && value != 1) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: split %d", value);
+            for (auto& c : b->classes) c.splitSweeps = value != 0;
+            break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: unknown option %d", option);
     }
     TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
@@ -847,6 +868,7 @@ extern "C" int tfx_batch_get_option(tfx_batch b, int option, int* value) {
         case TFX_BATCH_EXPANDED_GRIDS: *value = b->expandMode; break;
         case TFX_BATCH_OVERLAP_SDF: *value = b->overlap ? 1 : 0; break;
         case TFX_BATCH_SDF_BLOCK: *value = b->sdfL.constructThreads; break;
+        case TFX_BATCH_SPLIT_SWEEPS: *value = (!b->classes.empty() && b->classes[0].splitSweeps) ? 1 : 0; break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_get_option: unknown option %d", option);
     }
     return TFX_OK;

@@ -185,14 +185,21 @@ __global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __r
 // One block runs one group of GS = fused_group_strands(N) guide strands of one object at a time.
 // Shared memory, strand-major rows of N vertices padded to N+1 float4, so that both the one-lane-per-
 // strand sweep and the one-lane-per-vertex passes are free of bank conflicts:
-//   TP[GS][N+1] positions   TV[GS][N+1] Prev   TI[GS][N+1] InitialPos, then bind pose   TT[GS][N+1] tangents
-//   TR[GS][N] rest lengths  SK[GS][4] blended bone matrix rows   SL[GS][3] StrandLevelData
+//   TP[GS][N+1] positions   TI[GS][N+1] InitialPos, then the bind pose   TR[GS][N] rest lengths
+//   SK[GS][4] blended bone matrix rows   SL[GS][3] StrandLevelData
 //   one mbarrier, on which the bulk copies that bring a group's rows in complete.
+// Prev and Tangent never enter shared memory: each thread reads and writes its own vertices' words
+// in global memory (coalesced), which keeps a block small enough for five to fit per SM, and the
+// serial local-shape sweeps of that many groups to run side by side.
 __host__ __device__ constexpr int fused_group_strands(int n) { return n >= 64 ? 16 : 32; }
 __host__ __device__ constexpr int fused_smem_for(int n) {
-    return 4 * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * n * 4 + fused_group_strands(n) * 7 * 16 + 16;
+    return 2 * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * n * 4 + fused_group_strands(n) * 7 * 16 + 16;
 }
 constexpr int kFusedWaitPolls = 1 << 21;
+// k_fused_strands modes: the whole frame of the group, or its part before the local-shape sweeps
+// (integration, strand-level data, VSP; the state goes to global memory for k_local_sweep), or its
+// part after them (wind, length constraints, tangents, velocity clamp)
+constexpr int kFusedFull = 0, kFusedPre = 1, kFusedPost = 2;
 
 // IntegrationAndGlobalShapeConstraints (TressFXSimulation.hlsl:609-666) for vertex j: returns the new
 // position (after the global shape constraint) and, in `cur`, the position that becomes Prev.
@@ -284,17 +291,15 @@ __device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const f
 template <int N, int VPL>
 __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const BatchObject* __restrict__ objs,
                                                                         const WorkItem* __restrict__ items, int numItems,
-                                                                        int* err) {
+                                                                        int* err, int mode) {
     constexpr int GS = fused_group_strands(N);
     constexpr int RS = N + 1;       // tile row stride, float4
     constexpr int L = N / VPL;      // lanes per strand in the per-strand passes
     constexpr int SPW = 32 / L;     // strands per warp pass
     extern __shared__ float4 smem_f4[];
     float4* TP = smem_f4;
-    float4* TV = TP + GS * RS;
-    float4* TI = TV + GS * RS;
-    float4* TT = TI + GS * RS;
-    float* TR = reinterpret_cast<float*>(TT + GS * RS);
+    float4* TI = TP + GS * RS;
+    float* TR = reinterpret_cast<float*>(TI + GS * RS);
     float4* SK = reinterpret_cast<float4*>(TR + GS * N);
     float4* SL = SK + GS * 4;
     const uint32_t bar = smem_u32(SL + GS * 3);
@@ -320,16 +325,19 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
 
         // ------------------------------------------------------------ phase 0: bring the group in
         float4 bq4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool pre = mode != kFusedPost, post = mode != kFusedPre;   // phases 0-2 / phase 3 run
         if (warp == 0) {
-            if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)count * (uint32_t)(4 * N * 16 + N * 4));
+            // rows: Pos always; InitialPos for phases 0-2; RestLength for phase 3
+            const uint32_t rowBytes = N * 16 + (pre ? N * 16 : 0) + (post ? N * 4 : 0);
+            if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)count * rowBytes);
             __syncwarp();
             if (lane < count) {
                 const size_t vo = (size_t)(gs0 + lane * (F + 1)) * N;
                 bulk_g2s(smem_u32(TP + lane * RS), h.pos + vo, N * 16, bar);
-                bulk_g2s(smem_u32(TV + lane * RS), h.prev + vo, N * 16, bar);
-                bulk_g2s(smem_u32(TI + lane * RS), h.init + vo, N * 16, bar);
-                bulk_g2s(smem_u32(TT + lane * RS), h.tan + vo, N * 16, bar);
-                bulk_g2s(smem_u32(TR + lane * N), h.rest + vo, N * 4, bar);
+                if (pre) bulk_g2s(smem_u32(TI + lane * RS), h.init + vo, N * 16, bar);
+                if (post) bulk_g2s(smem_u32(TR + lane * N), h.rest + vo, N * 4, bar);
+            }
+            if (pre && lane < count) {
                 // strand level, while the rows are in flight: the blended bone matrix and its quaternion
                 const int gs = gs0 + lane * (F + 1);
                 float m[4][4];
@@ -348,7 +356,7 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
         }
 
         // ------------------------------------------------------------ phase 1a: CalculateStrandLevelData
-        if (warp == 0 && lane < count) {
+        if (pre && warp == 0 && lane < count) {
             const int s = lane, gs = gs0 + s * (F + 1);
             float m[4][4];
 #pragma unroll
@@ -357,8 +365,9 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
                 m[r][0] = row.x; m[r][1] = row.y; m[r][2] = row.z; m[r][3] = row.w;
             }
             float4 o0 = TP[s * RS], o1 = TP[s * RS + 1];
-            const float4 oo1 = TV[s * RS + 1];
-            const float4 n0 = integrate_vertex(c, m, TI[s * RS], o0, TV[s * RS], 0, N);
+            const size_t vo = (size_t)gs * N;
+            const float4 oo1 = h.prev[vo + 1];
+            const float4 n0 = integrate_vertex(c, m, TI[s * RS], o0, h.prev[vo], 0, N);
             const float4 n1 = integrate_vertex(c, m, TI[s * RS + 1], o1, oo1, 1, N);
             const float3 u = normalize(sub(xyz(o1), xyz(o0)));
             const float3 v = normalize(sub(xyz(n1), xyz(n0)));
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
         __syncthreads();
 
         // ------------------------------------------------------------ phase 1b: integration, VSP, bind pose
-        for (int e = tid; e < count * N; e += nthreads) {
+        for (int e = tid; pre && e < count * N; e += nthreads) {
             const int s = e / N, j = e % N;
             const int x = s * RS + j;
             float m[4][4];
@@ -390,10 +399,11 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
                 const float4 row = SK[s * 4 + r];
                 m[r][0] = row.x; m[r][1] = row.y; m[r][2] = row.z; m[r][3] = row.w;
             }
-            const float4 ip = TI[x], old = TV[x];
+            const size_t v = (size_t)(gs0 + s * (F + 1)) * N + j;
+            const float4 ip = TI[x], old = h.prev[v];
             float4 pv = TP[x];
             float4 p = integrate_vertex(c, m, ip, pv, old, j, N);
-            h.prevprev[(size_t)(gs0 + s * (F + 1)) * N + j] = old;
+            h.prevprev[v] = old;
             if (j >= 2) {
                 const float4 r4 = SL[s * 3 + 1], t4 = SL[s * 3 + 2];
                 const Q4 rot{r4.x, r4.y, r4.z, r4.w};
@@ -405,15 +415,26 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
                 pv = with_xyz(pv, b);
             }
             TP[x] = p;
-            TV[x] = pv;
-            const float4 b4 = SL[s * 3 + 0];
-            const float3 bp = qrot(Q4{b4.x, b4.y, b4.z, b4.w}, xyz(ip));
-            TI[x] = make_float4(bp.x, bp.y, bp.z, 0.0f);
+            h.prev[v] = pv;   // read back by phase 3 (after a block barrier)
+            if (mode == kFusedFull) {   // the bind pose, for the sweeps below
+                const float4 b4 = SL[s * 3 + 0];
+                const float3 bp = qrot(Q4{b4.x, b4.y, b4.z, b4.w}, xyz(ip));
+                TI[x] = make_float4(bp.x, bp.y, bp.z, 0.0f);
+            }
         }
         __syncthreads();
+        if (mode == kFusedPre) {
+            // the constrained-to-be state goes out; k_local_sweep and the kFusedPost pass take over
+            for (int e = tid; e < count * N; e += nthreads) {
+                const int s = e / N, j = e % N;
+                const int x = s * RS + j;
+                const size_t v = (size_t)(gs0 + s * (F + 1)) * N + j;
+                h.pos[v] = TP[x];
+            }
+        }
 
         // ------------------------------------------------------------ phase 2: LocalShapeConstraints
-        const int lsIters = c->reserved0;
+        const int lsIters = mode == kFusedFull ? c->reserved0 : 0;
         if (lsIters > 0) {
             const float stiff = 0.5f * fminf(c->localStiffness, 0.95f);
             for (int done = 0; done < lsIters;) {   // waves of up to one sweep per warp
@@ -426,19 +447,20 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
 
         // ------------------------------------------------------------ phase 3a: wind, length, tangents, clamp
         const float dt = c->timeStep;
-        for (int pass = warp; pass * SPW < count; pass += nwarps) {
+        for (int pass = warp; post && pass * SPW < count; pass += nwarps) {
             const int s = pass * SPW + slot;
             const bool active = s < count;
             const int gs = gs0 + s * (F + 1);
             const int base = s * RS + q * VPL;
+            const size_t vrow = (size_t)gs * N;   // the strand's first vertex
             float4 p[VPL], pv[VPL], tn[VPL];
             float len[VPL];
 #pragma unroll
             for (int k = 0; k < VPL; ++k) {
                 if (active) {
                     p[k] = TP[base + k];
-                    pv[k] = TV[base + k];
-                    tn[k] = TT[base + k];
+                    pv[k] = h.prev[vrow + q * VPL + k];
+                    tn[k] = h.tan[vrow + q * VPL + k];
                     len[k] = TR[s * N + q * VPL + k];
                 } else {
                     p[k] = pv[k] = tn[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -542,30 +564,108 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
                     pv[k] = with_xyz(pv[k], sub(xyz(p[k]), d));
                 }
             }
-            if (active) {
+            if (active) {   // the guide state goes out: Pos, Prev, Tangent
 #pragma unroll
                 for (int k = 0; k < VPL; ++k) {
-                    TP[base + k] = p[k];
-                    TV[base + k] = pv[k];
-                    TT[base + k] = tn[k];
+                    h.pos[vrow + q * VPL + k] = p[k];
+                    h.prev[vrow + q * VPL + k] = pv[k];
+                    h.tan[vrow + q * VPL + k] = tn[k];
                 }
             }
         }
         __syncthreads();
 
-        // ------------------------------------------------------------ phase 3c: write the guide state
-        // Pos / Prev / Tangent of the guides before collision; k_follow_collide adds the follow hairs
-        // and the collision once the frame's SDFs are built.
-        for (int e = tid; e < count * N; e += nthreads) {
-            const int s = e / N, j = e % N;
-            const int x = s * RS + j;
-            const size_t v = (size_t)(gs0 + s * (F + 1)) * N + j;
-            h.pos[v] = TP[x];
-            h.prev[v] = TV[x];
-            h.tan[v] = TT[x];
-        }
         fence_proxy_async_smem();   // this group's shared-memory accesses come before the next group's copies
         __syncthreads();
+    }
+}
+
+// ============================================================================================
+// LocalShapeConstraints (TressFXSimulation.hlsl:773-829) as the whole CPU re-dispatch loop
+// (TressFXSimulation.cpp:64-72), between the kFusedPre and kFusedPost passes: one thread per guide
+// strand, on the positions in global memory (each strand's rows stay in L1 across the sweep).  Up
+// to four consecutive sweeps run together as a wavefront inside the thread: sweep k works on vertex
+// j = t - 2k + 1 at step t, so it reads vertex j+1 as sweep k-1 left it one step earlier and vertex 1
+// as it left it two steps earlier -- registers handed from sweep to sweep, exactly the values the
+// sequential sweeps give -- and the four steps of one t are independent, so their latencies overlap.
+// More sweeps run in waves of four.  Many strands per SM (no shared-memory tiles) hide the rest.
+// The bind pose of vertex j is qrot(skinning quaternion, InitialPos_j), as phase 1b computes it.
+template <int N>
+__device__ __forceinline__ float3 bind_pose(const HairView& h, size_t vg, Q4 bq, int j) {
+    return qrot(bq, xyz(__ldg(h.init + vg + j)));
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) k_local_sweep(const BatchObject* __restrict__ objs,
+                                                     const WorkItem* __restrict__ items, int numItems) {
+    constexpr int GS = fused_group_strands(N);
+    constexpr int IPW = 32 / GS;     // work items per warp
+    constexpr int KMAX = 4;
+    const int lane = threadIdx.x & 31;
+    const int it = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * IPW + lane / GS;
+    if (it >= numItems) return;
+    const WorkItem wi = items[it];
+    const int s = lane % GS;
+    if (s >= wi.count) return;
+    const BatchObject& ob = objs[wi.obj];
+    const HairView h = ob.hair;
+    const DevSimConsts* __restrict__ c = ob.consts;
+    const int iters = c->reserved0;
+    if (iters <= 0) return;
+    const int gs = (wi.firstGuide + s) * (h.F + 1);
+    const size_t vg = (size_t)gs * N;
+    float4* __restrict__ P = h.pos + vg;
+    const float4 bq4 = h.sld[3 * gs];
+    const Q4 bq{bq4.x, bq4.y, bq4.z, bq4.w};
+    const float stiff = 0.5f * fminf(c->localStiffness, 0.95f);
+    const float4 p0 = P[0];          // vertex 0 is never moved by a sweep
+    const float3 b0v = bind_pose<N>(h, vg, bq, 0), b1v = bind_pose<N>(h, vg, bq, 1);
+    for (int done = 0; done < iters; done += KMAX) {
+        const int K = min(iters - done, KMAX);
+        float4 pm1[KMAX], cur[KMAX], o1[KMAX], o2[KMAX];
+        float3 bm1[KMAX], b0[KMAX];
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k) {
+            pm1[k] = cur[k] = o1[k] = o2[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            bm1[k] = b0[k] = mk3(0.f, 0.f, 0.f);
+        }
+        const int T = (N - 2) + 2 * (K - 1);
+        for (int t = 0; t < T; ++t) {
+            float4 out[KMAX];
+#pragma unroll
+            for (int k = 0; k < KMAX; ++k) {
+                out[k] = o1[k];
+                if (k >= K) continue;
+                const int j = t - 2 * k + 1;
+                if (j >= 1 && j <= N - 2) {
+                    if (j == 1) {
+                        pm1[k] = p0;
+                        cur[k] = k == 0 ? P[1] : o2[k - 1];   // vertex 1 as sweep k-1 left it
+                        bm1[k] = b0v;
+                        b0[k] = b1v;
+                    }
+                    float4 pp1 = k == 0 ? P[j + 1] : o1[k - 1];   // vertex j+1 as sweep k-1 left it
+                    const float3 bp1 = bind_pose<N>(h, vg, bq, j + 1);
+                    local_shape_step(pm1[k], cur[k], pp1, bm1[k], b0[k], bp1, stiff);
+                    out[k] = cur[k];
+                    if (k == K - 1) {
+                        P[j] = cur[k];
+                        if (j == N - 2) P[N - 1] = pp1;
+                    }
+                    pm1[k] = cur[k];
+                    cur[k] = pp1;
+                    bm1[k] = b0[k];
+                    b0[k] = bp1;
+                } else if (j == N - 1) {
+                    out[k] = cur[k];   // vertex N-1 after the sweep's last step
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < KMAX; ++k) {
+                o2[k] = o1[k];
+                o1[k] = out[k];
+            }
+        }
     }
 }
 
@@ -641,7 +741,6 @@ __device__ __forceinline__ bool follow_group(const BatchObject& ob, const WorkIt
 // Guide vertex e of a group: its follow vertices and the collision of all of them.
 template <int N>
 __device__ __forceinline__ void follow_collide_vertex(const FollowGroup& fg, int e) {
-    constexpr int U = 4;   // the near-vertex loop below selects among exactly four
     constexpr float kInvN = 1.0f / (float)N;   // exact: N is a power of two, so j * kInvN == j / N
     const HairView& h = fg.h;
     const int F = h.F;
@@ -656,60 +755,29 @@ __device__ __forceinline__ void follow_collide_vertex(const FollowGroup& fg, int
     const float4 tn = h.tan[vg];
     const bool collide = sdf && j >= 2;
     const float factor = tip * ((float)j * kInvN) + 1.0f;
-    for (int i0 = 0; i0 <= F; i0 += U) {
-        float3 pt[U];
-        float wU[U], dist[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int i = i0 + u;
-            pt[u] = xyz(gp);
-            wU[u] = gp.w;
-            if (i > 0 && i <= F) {
-                const float4 off = __ldg(h.followOffset + gs + i);
-                pt[u] = add(xyz(gp), mul(factor, xyz(off)));
-                // inverse mass of the follow vertex: only this thread writes the word, after this read
-                wU[u] = __ldg(&h.pos[vg + (size_t)i * N].w);
-            }
+    for (int i = 0; i <= F; ++i) {
+        const size_t v = vg + (size_t)i * N;
+        float3 pt = xyz(gp);
+        float w = gp.w;
+        if (i > 0) {
+            const float4 off = __ldg(h.followOffset + gs + i);
+            pt = add(xyz(gp), mul(factor, xyz(off)));
+            // inverse mass of the follow vertex: only this thread writes the word, after this read
+            w = __ldg(&h.pos[v].w);
         }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            dist[u] = 1e10f;
-            if (collide && i0 + u <= F) dist[u] = sdf8 ? sdf_lookup8(sdf8, sg, pt[u]) : sdf_lookup(sdf, sg, pt[u]);
+        float3 proj = pt;
+        bool hit = false;
+        if (collide) {
+            const float dist = sdf8 ? sdf_lookup8(sdf8, sg, pt) : sdf_lookup(sdf, sg, pt);
+            if (dist <= margin) hit = collide_near(sdf, sdf8, sg, margin, pt, dist, &proj);
         }
-        // vertices beyond the margin are final; the few within it run the gradient part in one loop
-        // (one copy of that code, not U)
-        unsigned near = 0;
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int i = i0 + u;
-            if (i > F) continue;
-            if (collide && dist[u] <= margin) {
-                near |= 1u << u;
-                continue;
-            }
-            if (i > 0) {
-                h.pos[vg + (size_t)i * N] = make_float4(pt[u].x, pt[u].y, pt[u].z, wU[u]);
-                h.tan[vg + (size_t)i * N] = tn;
-            }
+        if (i > 0) {
+            h.pos[v] = make_float4(proj.x, proj.y, proj.z, w);
+            h.tan[v] = tn;
+        } else if (hit) {
+            h.pos[v] = with_xyz(gp, proj);
         }
-        while (near) {
-            const int u = __ffs(near) - 1;
-            near &= near - 1;
-            const int i = i0 + u;
-            const float3 p = u == 0 ? pt[0] : (u == 1 ? pt[1] : (u == 2 ? pt[2] : pt[3]));
-            const float d = u == 0 ? dist[0] : (u == 1 ? dist[1] : (u == 2 ? dist[2] : dist[3]));
-            const float w = u == 0 ? wU[0] : (u == 1 ? wU[1] : (u == 2 ? wU[2] : wU[3]));
-            const size_t v = vg + (size_t)i * N;
-            float3 proj = p;
-            const bool hit = collide_near(sdf, sdf8, sg, margin, p, d, &proj);
-            if (i > 0) {
-                h.pos[v] = make_float4(hit ? proj.x : p.x, hit ? proj.y : p.y, hit ? proj.z : p.z, w);
-                h.tan[v] = tn;
-            } else if (hit) {
-                h.pos[v] = with_xyz(gp, proj);
-            }
-            if (hit) h.prev[v] = with_xyz(h.prev[v], proj);
-        }
+        if (hit) h.prev[v] = with_xyz(h.prev[v], proj);
     }
 }
 
@@ -720,13 +788,14 @@ __device__ __forceinline__ void follow_collide_vertex(const FollowGroup& fg, int
 // (TressFXSDFCollision.hlsl:531-595) for the groups of one vertices-per-strand class, after
 // k_fused_strands has written the guides' constrained state and the frame's SDFs are built.  One
 // thread per guide vertex; it makes the vertex's F follow vertices (hair i = 1..F) from the guide's
-// pre-collision position, then collides the guide vertex and every follow vertex.  The loads of U
-// hairs are issued before any of them is collided or written, so their latencies overlap.  Each group
+// pre-collision position, then collides the guide vertex and every follow vertex (one vertex at a
+// time: at 64 registers four blocks fit per SM, and that occupancy hides the gathers better than
+// loads of several hairs in flight per thread did).  Each group
 // is cut into chunksPerItem chunks of guide vertices (a multiple of 256), which persistent blocks take
 // in turn: with few groups per block, smaller chunks spread groups of unequal cost (collisions) evenly
 // over the SMs; with many, whole groups keep the per-chunk overhead low.
 template <int N>
-__global__ void __launch_bounds__(256, 3) k_follow_collide(const BatchObject* __restrict__ objs,
+__global__ void __launch_bounds__(256, 4) k_follow_collide(const BatchObject* __restrict__ objs,
                                                            const WorkItem* __restrict__ items, int numItems,
                                                            int chunksPerItem) {
     constexpr int kGroupVerts = fused_group_strands(N) * N;
@@ -749,7 +818,7 @@ template <int N, int VPL>
 static cudaError_t launch_fused_nv(const FusedLaunch& fl, cudaStream_t s) {
     // the dynamic shared-memory attribute is set by fused_blocks_per_sm before the first launch
     k_fused_strands<N, VPL><<<fl.blocks, fl.warpsPerBlock * 32, fused_smem_for(N), s>>>(fl.objs, fl.items, fl.numItems,
-                                                                                        fl.err);
+                                                                                        fl.err, fl.mode);
     return cudaGetLastError();
 }
 
@@ -762,6 +831,26 @@ bool fused_config_valid(int n, int vpl) {
 }
 
 int fused_smem_bytes(int n, int, int) { return fused_smem_for(n); }
+
+template <int N>
+static cudaError_t launch_sweep_n(const FusedLaunch& fl, cudaStream_t s) {
+    constexpr int IPW = 32 / fused_group_strands(N);
+    const long long threads = (long long)((fl.numItems + IPW - 1) / IPW) * 32;
+    k_local_sweep<N><<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(fl.objs, fl.items, fl.numItems);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_local_sweep(const FusedLaunch& fl, cudaStream_t s) {
+    if (fl.numItems <= 0) return cudaSuccess;
+    switch (fl.n) {
+        case 4: return launch_sweep_n<4>(fl, s);
+        case 8: return launch_sweep_n<8>(fl, s);
+        case 16: return launch_sweep_n<16>(fl, s);
+        case 32: return launch_sweep_n<32>(fl, s);
+        case 64: return launch_sweep_n<64>(fl, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
 int fused_group_size(int n) { return fused_group_strands(n); }
 
 #define TFX_FUSED_CASE(NN, VV) \
