@@ -360,13 +360,17 @@ typedef enum tfx_batch_option {
                                        passes of the strand kernel; 0: inside the strand kernel      */
 } tfx_batch_option;
 /* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
- * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (float4 per
- * vertex; pinned memory copies fastest).  The call queues a device snapshot on the context's stream
- * and its copy to the host on a separate copy stream, so the copy overlaps the next frames; it
- * returns at once with a ticket.  The destination must stay valid and untouched until
- * tfx_batch_wait_readback(ticket) returns.  No counterpart in the reference (its renderer reads the
- * buffers on the GPU); this is how a host consumer takes frames without stalling the simulation. */
-int tfx_batch_readback(tfx_batch batch, void* const* host_dst, int count, int64_t* ticket);
+ * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (format
+ * TFX_READBACK_XYZW: the float4 of the position buffer) or num_vertices * 12 bytes (TFX_READBACK_XYZ:
+ * x, y, z packed; w is the inverse mass, which the simulation never changes).  Pinned memory copies
+ * fastest.  The call queues a device snapshot on the context's stream and its copy to the host on a
+ * separate copy stream, so the copy overlaps the next frames; it returns at once with a ticket.  The
+ * destination must stay valid and untouched until tfx_batch_wait_readback(ticket) returns.  No
+ * counterpart in the reference (its renderer reads the buffers on the GPU); this is how a host
+ * consumer takes frames without stalling the simulation. */
+#define TFX_READBACK_XYZW 0
+#define TFX_READBACK_XYZ 1
+int tfx_batch_readback(tfx_batch batch, void* const* host_dst, int count, int format, int64_t* ticket);
 int tfx_batch_wait_readback(tfx_batch batch, int64_t ticket);
 int tfx_batch_set_option(tfx_batch batch, int option, int value);
 int tfx_batch_get_option(tfx_batch batch, int option, int* value);

@@ -179,30 +179,42 @@ def test_batched_follow_collide_many_contacts_bit_exact(ctx, follows):
 
 
 @pytest.mark.gpu
-def test_batched_readback_delivers_each_frame(ctx):
-    """tfx_batch_readback: the positions after each frame reach host memory bit for bit while later
-    frames run; bad tickets and destination counts are refused."""
+@pytest.mark.parametrize("fmt", [0, 1])
+def test_batched_readback_delivers_each_frame(ctx, fmt):
+    """tfx_batch_readback: the positions after each frame (float4, or packed xyz) reach host memory bit
+    for bit while later frames run; bad tickets, formats and destination counts are refused."""
     from tressfx_gb300.api import PinnedArray
     sc = scene_head(seed=31, num_guides=200, n=16, follows=2, triangles=2500, sdf_cells=40, frames=6)
+    sc2 = scene_small(seed=3, num_guides=100, n=8)
+    sc.objects.append(sc2.objects[0])
     gpu = BatchedPipeline(ctx, sc)
-    bufs = [[PinnedArray((h.num_vertices, 4), np.float32) for h in gpu.hair] for _ in range(3)]
+    width = 4 if fmt == 0 else 3
+    bufs = [[PinnedArray((h.num_vertices, width), np.float32) for h in gpu.hair] for _ in range(3)]
     try:
         tickets, want = [], []
+
+        def check(f):
+            for o in range(len(gpu.hair)):
+                got = bufs[f % 3][o].array
+                assert np.array_equal(got.view(np.uint32), want[f][o][:, :width].view(np.uint32)), (f, o)
+
         for f in range(6):
             gpu.step(f)
-            tickets.append(gpu.batch.readback([b.array.ctypes.data for b in bufs[f % 3]]))
+            tickets.append(gpu.batch.readback([b.array.ctypes.data for b in bufs[f % 3]], fmt))
             if f >= 2:
                 gpu.batch.wait_readback(tickets[f - 2])
-                assert np.array_equal(bufs[(f - 2) % 3][0].array.view(np.uint32), want[f - 2].view(np.uint32)), f
+                check(f - 2)
             ctx.synchronize()
-            want.append(gpu.hair[0].read(A.BUF_POSITIONS).copy())
+            want.append([np.ascontiguousarray(h.read(A.BUF_POSITIONS).reshape(-1, 4)) for h in gpu.hair])
         for f in (4, 5):
             gpu.batch.wait_readback(tickets[f])
-            assert np.array_equal(bufs[f % 3][0].array.view(np.uint32), want[f].view(np.uint32)), f
+            check(f)
         with pytest.raises(Exception):
             gpu.batch.wait_readback(99)
         with pytest.raises(Exception):
             gpu.batch.readback([])
+        with pytest.raises(Exception):
+            gpu.batch.readback([b.array.ctypes.data for b in bufs[0]], 7)
     finally:
         for side in bufs:
             for b in side:

@@ -204,7 +204,7 @@ _PROTOS = {
     "tfx_nsdf_get_info": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_int32)]),
     "tfx_batch_create": (C.c_int, [P, C.POINTER(P)]),
-    "tfx_batch_readback": (C.c_int, [P, C.POINTER(P), C.c_int, C.POINTER(C.c_int64)]),
+    "tfx_batch_readback": (C.c_int, [P, C.POINTER(P), C.c_int, C.c_int, C.POINTER(C.c_int64)]),
     "tfx_batch_wait_readback": (C.c_int, [P, C.c_int64]),
     "tfx_batch_destroy": (C.c_int, [P]),
     "tfx_batch_add_sdf": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),

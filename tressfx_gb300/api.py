@@ -432,11 +432,14 @@ class Batch:
     def run(self) -> None:
         check(A.lib().tfx_batch_run(self.handle), "tfx_batch_run")
 
-    def readback(self, host_ptrs: list[int]) -> int:
-        """Queues the copy of every hair object's positions into host memory; returns a ticket."""
+    READBACK_XYZW, READBACK_XYZ = 0, 1
+
+    def readback(self, host_ptrs: list[int], fmt: int = 0) -> int:
+        """Queues the copy of every hair object's positions into host memory (float4, or packed xyz with
+        fmt = READBACK_XYZ); returns a ticket."""
         arr = (C.c_void_p * len(host_ptrs))(*host_ptrs)
         tk = C.c_int64()
-        check(A.lib().tfx_batch_readback(self.handle, arr, len(host_ptrs), C.byref(tk)), "tfx_batch_readback")
+        check(A.lib().tfx_batch_readback(self.handle, arr, len(host_ptrs), int(fmt), C.byref(tk)), "tfx_batch_readback")
         return tk.value
 
     def wait_readback(self, ticket: int) -> None:

@@ -86,6 +86,9 @@ cudaError_t launch_local_sweep(const FusedLaunch& fl, cudaStream_t s);
 cudaError_t launch_follow_collide(const FollowLaunch& fl, cudaStream_t s);
 cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s);
 cudaError_t launch_batch_sdf(const SdfBatchLaunch& l, cudaStream_t s);
+// Every object's positions, consecutively (first[i] = object i's first vertex), into `out` as float4 or packed xyz.
+cudaError_t launch_snapshot_positions(const BatchObject* objs, const long long* first, int nobj, long long total,
+                                      float* out, int xyzOnly, cudaStream_t s);
 bool fused_config_valid(int n, int vpl);
 int fused_smem_bytes(int n, int vpl, int warps);
 int fused_blocks_per_sm(int n, int vpl, int warps);

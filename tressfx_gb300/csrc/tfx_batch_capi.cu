@@ -88,8 +88,9 @@ struct tfx_batch_t {
     // `copy` while the next frames run
     cudaStream_t copy = nullptr;
     char* snap[2] = {nullptr, nullptr};
-    std::vector<size_t> snapOff;     // per hair object: offset in a snapshot
-    size_t snapBytes = 0;
+    std::vector<long long> snapFirst;  // per hair object: its first vertex in a snapshot
+    long long* devFirst = nullptr;     // the same, on the device
+    long long snapVerts = 0;
     cudaEvent_t snapDone[2] = {nullptr, nullptr}, copyDone[2] = {nullptr, nullptr};
     bool copyUsed[2] = {false, false};
     int64_t nextTicket = 0;
@@ -123,6 +124,7 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
         if (b->copyDone[i]) cudaEventDestroy(b->copyDone[i]);
     }
     if (b->copy) cudaStreamDestroy(b->copy);
+    if (b->devFirst) cudaFree(b->devFirst);
     if (b->pinnedErr) cudaFreeHost(b->pinnedErr);
     if (b->evFork) cudaEventDestroy(b->evFork);
     if (b->evJoin) cudaEventDestroy(b->evJoin);
@@ -753,25 +755,30 @@ extern "C" int tfx_batch_run(tfx_batch b) {
 
 static int readback_init(tfx_batch b) {
     if (b->copy) return TFX_OK;
-    b->snapOff.assign(b->hairs.size(), 0);
-    size_t off = 0;
+    b->snapFirst.assign(b->hairs.size(), 0);
+    long long v = 0;
     for (size_t i = 0; i < b->hairs.size(); ++i) {
-        b->snapOff[i] = off;
-        off += ((size_t)b->hairs[i]->Vtot * sizeof(float4) + 255) & ~(size_t)255;
+        b->snapFirst[i] = v;
+        v += b->hairs[i]->Vtot;
     }
-    b->snapBytes = off;
+    b->snapVerts = v;
     for (int i = 0; i < 2; ++i) {
-        TFX_CUDA(cudaMalloc(&b->snap[i], std::max<size_t>(off, 256)), "tfx_batch_readback: snapshot buffer");
+        TFX_CUDA(cudaMalloc(&b->snap[i], std::max<size_t>((size_t)v * sizeof(float4), 256)), "tfx_batch_readback: snapshot buffer");
         TFX_CUDA(cudaEventCreateWithFlags(&b->snapDone[i], cudaEventDisableTiming), "cudaEventCreate");
         TFX_CUDA(cudaEventCreateWithFlags(&b->copyDone[i], cudaEventDisableTiming), "cudaEventCreate");
     }
+    TFX_CUDA(cudaMalloc(&b->devFirst, sizeof(long long) * std::max<size_t>(b->hairs.size(), 1)), "tfx_batch_readback: table");
+    TFX_CUDA(cudaMemcpy(b->devFirst, b->snapFirst.data(), sizeof(long long) * b->hairs.size(), cudaMemcpyHostToDevice),
+             "tfx_batch_readback: table");
     TFX_CUDA(cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking), "tfx_batch_readback: copy stream");
     return TFX_OK;
 }
 
-extern "C" int tfx_batch_readback(tfx_batch b, void* const* host_dst, int count, int64_t* ticket) {
+extern "C" int tfx_batch_readback(tfx_batch b, void* const* host_dst, int count, int format, int64_t* ticket) {
     if (!b || !host_dst || !ticket) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: null argument");
     if (!b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: batch not built");
+    if (format != TFX_READBACK_XYZW && format != TFX_READBACK_XYZ)
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: format %d", format);
     if (count != (int)b->hairs.size())
         return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_readback: %d destinations for %d hair objects", count,
                     (int)b->hairs.size());
@@ -781,19 +788,18 @@ extern "C" int tfx_batch_readback(tfx_batch b, void* const* host_dst, int count,
     if (int r = readback_init(b)) return r;
     const int64_t t = b->nextTicket;
     const int s = (int)(t & 1);
+    const size_t per = format == TFX_READBACK_XYZ ? 3 * sizeof(float) : sizeof(float4);
     cudaStream_t main = b->ctx->stream;
     // the snapshot may not overwrite a buffer whose copy to the host is still running
     if (b->copyUsed[s]) TFX_CUDA(cudaStreamWaitEvent(main, b->copyDone[s], 0), "cudaStreamWaitEvent");
-    for (int i = 0; i < count; ++i) {
-        tfx_hair h = b->hairs[i];
-        TFX_CUDA(cudaMemcpyAsync(b->snap[s] + b->snapOff[i], h->view.pos, (size_t)h->Vtot * sizeof(float4),
-                                 cudaMemcpyDeviceToDevice, main), "tfx_batch_readback: snapshot");
-    }
+    cudaError_t e = launch_snapshot_positions(b->objTable, b->devFirst, count, b->snapVerts,
+                                              reinterpret_cast<float*>(b->snap[s]), format == TFX_READBACK_XYZ, main);
+    if (e != cudaSuccess) return cuda_fail(e, "tfx_batch_readback: snapshot");
     TFX_CUDA(cudaEventRecord(b->snapDone[s], main), "cudaEventRecord");
     TFX_CUDA(cudaStreamWaitEvent(b->copy, b->snapDone[s], 0), "cudaStreamWaitEvent");
     for (int i = 0; i < count; ++i) {
         tfx_hair h = b->hairs[i];
-        TFX_CUDA(cudaMemcpyAsync(host_dst[i], b->snap[s] + b->snapOff[i], (size_t)h->Vtot * sizeof(float4),
+        TFX_CUDA(cudaMemcpyAsync(host_dst[i], b->snap[s] + (size_t)b->snapFirst[i] * per, (size_t)h->Vtot * per,
                                  cudaMemcpyDeviceToHost, b->copy), "tfx_batch_readback: copy to host");
     }
     TFX_CUDA(cudaEventRecord(b->copyDone[s], b->copy), "cudaEventRecord");

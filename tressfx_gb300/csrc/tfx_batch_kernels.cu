@@ -630,7 +630,17 @@ __global__ void __launch_bounds__(128) k_local_sweep(const BatchObject* __restri
             bm1[k] = b0[k] = mk3(0.f, 0.f, 0.f);
         }
         const int T = (N - 2) + 2 * (K - 1);
+        // sweep 0 reads vertex t+2 (position and InitialPos) at step t: those loads are issued two steps
+        // ahead (a miss costs an L2 round trip, which two steps cover); the later sweeps read
+        // InitialPos rows that sweep 0 brought into L1.  Indices past the strand's end are clamped.
+        float4 qP0 = P[min(2, N - 1)], qP1 = P[min(3, N - 1)];
+        float4 qI0 = __ldg(h.init + vg + min(2, N - 1)), qI1 = __ldg(h.init + vg + min(3, N - 1));
         for (int t = 0; t < T; ++t) {
+            const float4 pAhead = qP0, iAhead = qI0;   // vertex t+2
+            qP0 = qP1;
+            qI0 = qI1;
+            qP1 = P[min(t + 4, N - 1)];
+            qI1 = __ldg(h.init + vg + min(t + 4, N - 1));
             float4 out[KMAX];
 #pragma unroll
             for (int k = 0; k < KMAX; ++k) {
@@ -644,8 +654,8 @@ __global__ void __launch_bounds__(128) k_local_sweep(const BatchObject* __restri
                         bm1[k] = b0v;
                         b0[k] = b1v;
                     }
-                    float4 pp1 = k == 0 ? P[j + 1] : o1[k - 1];   // vertex j+1 as sweep k-1 left it
-                    const float3 bp1 = bind_pose<N>(h, vg, bq, j + 1);
+                    float4 pp1 = k == 0 ? pAhead : o1[k - 1];   // vertex j+1 as sweep k-1 left it
+                    const float3 bp1 = k == 0 ? qrot(bq, xyz(iAhead)) : bind_pose<N>(h, vg, bq, j + 1);
                     local_shape_step(pm1[k], cur[k], pp1, bm1[k], b0[k], bp1, stiff);
                     out[k] = cur[k];
                     if (k == K - 1) {
@@ -810,6 +820,35 @@ __global__ void __launch_bounds__(256, 4) k_follow_collide(const BatchObject* __
         if (!follow_group(objs[wi.obj], wi, fg)) continue;
         for (int e = begin + (int)threadIdx.x; e < end; e += blockDim.x) follow_collide_vertex<N>(fg, e);
     }
+}
+
+// ============================================================================================
+// readback snapshot: every object's positions, one after the other, as float4 (xyzw) or packed xyz
+__global__ void __launch_bounds__(256) k_snapshot_positions(const BatchObject* __restrict__ objs,
+                                                            const long long* __restrict__ first, int nobj,
+                                                            long long total, float* __restrict__ out, int xyzOnly) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += stride) {
+        int lo = 0, hi = nobj - 1;
+        while (lo < hi) {   // last object whose first vertex <= t
+            const int mid = (lo + hi + 1) >> 1;
+            if (first[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        const float4 p = objs[lo].hair.pos[t - first[lo]];
+        if (xyzOnly) {
+            out[3 * t] = p.x; out[3 * t + 1] = p.y; out[3 * t + 2] = p.z;
+        } else {
+            reinterpret_cast<float4*>(out)[t] = p;
+        }
+    }
+}
+
+cudaError_t launch_snapshot_positions(const BatchObject* objs, const long long* first, int nobj, long long total,
+                                      float* out, int xyzOnly, cudaStream_t s) {
+    if (total <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, 152LL * 16);
+    k_snapshot_positions<<<blocks, 256, 0, s>>>(objs, first, nobj, total, out, xyzOnly);
+    return cudaGetLastError();
 }
 
 // ============================================================================================
