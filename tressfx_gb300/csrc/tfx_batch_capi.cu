@@ -30,7 +30,7 @@ using namespace tfx;
 
 struct BatchClass {
     int n = 0;
-    int vpl = 1, warps = 8, blocks = 1;
+    int vpl = 2, warps = 4, blocks = 1;
     int perSMCap = 0;            // resident strand blocks per SM allowed (0 = as many as fit)
     int followBlocks = 1;        // grid of k_follow_collide (persistent over the chunks)
     int followChunks = 1;        // chunks per group in k_follow_collide
@@ -457,31 +457,33 @@ static int autotune(tfx_batch b, int frames) {
         BatchClass& c = b->classes[ci];
         if (c.numItems == 0) continue;
         int bestV = c.vpl, bestW = c.warps, bestCap = c.perSMCap;
-        for (int vpl : {1, 2, 4}) {
-            if (!fused_config_valid(c.n, vpl)) continue;
-            for (int warps : {4, 8}) {
-                const int perSM = fused_blocks_per_sm(c.n, vpl, warps);
-                if (perSM <= 0) continue;
-                for (int cap = perSM; cap >= std::max(1, perSM - 1); --cap) {
-                    if (vpl == bestV && warps == bestW && (cap == perSM ? 0 : cap) == bestCap) continue;
-                    c.vpl = vpl; c.warps = warps; c.perSMCap = cap == perSM ? 0 : cap;
-                    if ((rc = size_class(b, c))) break;
-                    float ms;
-                    if ((rc = time_graph_frames(b, frames, &ms))) break;
-                    if (ms < best) { best = ms; bestV = vpl; bestW = warps; bestCap = c.perSMCap; }
+        bool bestSplit = c.splitSweeps;
+        for (int split = 0; split < 2 && rc == TFX_OK; ++split) {   // sweeps inside, or their own launch
+            for (int vpl : {1, 2, 4}) {
+                if (!fused_config_valid(c.n, vpl)) continue;
+                for (int warps : {4, 8}) {
+                    const int perSM = fused_blocks_per_sm(c.n, vpl, warps);
+                    if (perSM <= 0) continue;
+                    for (int cap = perSM; cap >= std::max(1, perSM - 1); --cap) {
+                        if ((split != 0) == bestSplit && vpl == bestV && warps == bestW &&
+                            (cap == perSM ? 0 : cap) == bestCap)
+                            continue;
+                        c.splitSweeps = split != 0;
+                        c.vpl = vpl; c.warps = warps; c.perSMCap = cap == perSM ? 0 : cap;
+                        if ((rc = size_class(b, c))) break;
+                        float ms;
+                        if ((rc = time_graph_frames(b, frames, &ms))) break;
+                        if (ms < best) {
+                            best = ms; bestV = vpl; bestW = warps; bestCap = c.perSMCap; bestSplit = split != 0;
+                        }
+                    }
+                    if (rc) break;
                 }
                 if (rc) break;
             }
-            if (rc) break;
         }
-        c.vpl = bestV; c.warps = bestW; c.perSMCap = bestCap;
+        c.vpl = bestV; c.warps = bestW; c.perSMCap = bestCap; c.splitSweeps = bestSplit;
         if (rc == TFX_OK) rc = size_class(b, c);
-        if (rc == TFX_OK) {   // the sweeps in the strand kernel, or as their own launch
-            c.splitSweeps = !c.splitSweeps;
-            float ms;
-            if ((rc = time_graph_frames(b, frames, &ms)) == TFX_OK && !(ms < best)) c.splitSweeps = !c.splitSweeps;
-            else if (rc == TFX_OK) best = ms;
-        }
     }
     int rr = snapshot_restore(sn, s);
     return rc ? rc : rr;
@@ -645,9 +647,7 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         if (!any) continue;
         BatchClass c;
         c.n = n;
-        c.vpl = n <= 32 ? 1 : 2;
-        c.warps = 8;
-        make_items(b, c);
+        make_items(b, c);   // vpl / warps: the BatchClass defaults (what the autotuner picks on the head and fur workloads)
         if (int r = upload_items(c)) return r;
         if (int r = size_class(b, c)) return r;
         b->classes.push_back(std::move(c));
