@@ -12,6 +12,7 @@
 
 #include "tressfx/TressFXBoneSkinning.h"
 #include "tressfx/TressFXSDFCollision.h"
+#include "tressfx/TressFXSDFMarchingCubes.h"
 #include "tressfx/TressFXSimulation.h"
 
 namespace {
@@ -124,6 +125,16 @@ int main(int argc, char** argv) {
         std::vector<char> grid((size_t)sdf.GetGridNumTotalCells() * 4);
         if (tfx_sdf_read(sdf.GetHandle(), grid.data(), grid.size()) != TFX_OK) return 9;
         put("out_sdf", grid.data(), grid.size());
+        // the iso-surface of the last frame's grid at the collision margin (src/SDF.cpp:63)
+        TressFXSDFMarchingCubes mc(1 << 17);
+        mc.Initialize("mesh", &device);
+        mc.SetSDF(&sdf);
+        mc.SetSDFIsoLevel(sdf.GetSDFCollisionMargin());
+        mc.Update(cc);
+        std::vector<float> mcv;
+        const int mcCount = mc.ReadVertices(mcv);
+        put("mc_count", &mcCount, sizeof(int));
+        put("mc_vertices", mcv.data(), mcv.size() * sizeof(float));
         const auto stamps = device.GetTimeStamps();
         std::string names_joined;
         for (auto& st : stamps) names_joined += st.first + "\n";

@@ -118,6 +118,15 @@ def test_cpp_host_classes_match_python_mirror(ctx, host_sim, tmp_path):
         assert np.array_equal(got, want), f"{name}: {int((got != want).sum())} words differ"
     cells = int(grids[-1, 4] * grids[-1, 5] * grids[-1, 6])
     assert np.array_equal(np.frombuffer(d["out_sdf"], np.uint32)[:cells], sdf.read(cells))
+    # TressFXSDFMarchingCubes on the last grid, at the collision margin, against tfx_mc through Python
+    from tressfx_gb300.api import SDFMarchingCubes
+    mc = SDFMarchingCubes(ctx, 1 << 17, alloc)
+    mc.set_iso_level(float(grids[-1, 7]))
+    mc.update(sdf, g)
+    want_v, want_n = mc.read()
+    assert int(np.frombuffer(d["mc_count"], np.int32)[0]) == want_n and want_n > 100
+    assert np.array_equal(np.frombuffer(d["mc_vertices"], np.uint32), want_v.view(np.uint32).reshape(-1))
+    mc.close()
     assert (sdf.read(cells).view(np.float32) < 1e10).sum() > 1000
     pos = hair.read(A.BUF_POSITIONS)
     assert np.isfinite(pos).all()
