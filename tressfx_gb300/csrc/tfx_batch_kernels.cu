@@ -150,32 +150,7 @@ __global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __r
         const float3 x0 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 0)));
         const float3 x1 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 1)));
         const float3 x2 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 2)));
-        int3 lo, hi;
-        tri_cell_box(g, x0, x1, x2, lo, hi);
-        const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
-        const int nxy = nx * ny;
-        const int vol = nxy * nz;
-        const TriPre P = tri_pre(x0, x1, x2);
-        // Box coordinates of c.  (c + 0.5) / m lies at least 0.5 / m from an integer, and the float
-        // product (c + 0.5) * (1 / m) is within (c / m) * 2^-23 of it, so its truncation is the
-        // integer quotient while c < 2^22; larger boxes use integer division.
-        const bool floatIdx = vol < (1 << 22);
-        const float inxy = 1.0f / (float)nxy, inx = 1.0f / (float)nx;
-        for (int c = lane; c < vol; c += 32) {
-            int cz, r, cy;
-            if (floatIdx) {
-                cz = (int)(((float)c + 0.5f) * inxy);
-                r = c - cz * nxy;
-                cy = (int)(((float)r + 0.5f) * inx);
-            } else {
-                cz = c / nxy;
-                r = c - cz * nxy;
-                cy = r / nx;
-            }
-            const int x = lo.x + (r - cy * nx), y = lo.y + cy, z = lo.z + cz;
-            const float d = signed_dist_pre(sdf_cell_pos(g, x, y, z), P);
-            atomicMin(s.words + ((long long)z * g.ny + y) * g.nx + x, float_flip3(d));
-        }
+        sdf_construct_triangle_warp(s.words, g, x0, x1, x2, lane);
     }
 }
 

@@ -20,28 +20,19 @@ __global__ void __launch_bounds__(256) k_sdf_initialize(uint32_t* __restrict__ s
     for (long long i = (n4 << 2) + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells; i += stride) sdf[i] = v;
 }
 
-// ConstructSignedDistanceField, :329-397.  One thread per triangle.
+// ConstructSignedDistanceField, :329-397.  One warp per triangle (sdf_construct_triangle_warp); the
+// warps stride over the triangles.
 __global__ void __launch_bounds__(128) k_sdf_construct(uint32_t* __restrict__ sdf, SdfGrid g,
                                                        const float4* __restrict__ mesh,
                                                        const uint32_t* __restrict__ idx, int ntri) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntri) return;
-    const float3 tri0 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 0)));
-    const float3 tri1 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 1)));
-    const float3 tri2 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 2)));
-    const float3 m = mk3(g.cell, g.cell, g.cell);
-    const float3 aabbMin = sub(vmin(tri0, vmin(tri1, tri2)), m);
-    const float3 aabbMax = add(vmax(tri0, vmax(tri1, tri2)), m);
-    int3 lo = sdf_coords(g, aabbMin), hi = sdf_coords(g, aabbMax);
-    lo.x = max(0, min(lo.x - 1, g.nx - 1)); lo.y = max(0, min(lo.y - 1, g.ny - 1)); lo.z = max(0, min(lo.z - 1, g.nz - 1));
-    hi.x = max(0, min(hi.x + 1, g.nx - 1)); hi.y = max(0, min(hi.y + 1, g.ny - 1)); hi.z = max(0, min(hi.z + 1, g.nz - 1));
-    for (int z = lo.z; z <= hi.z; ++z)
-        for (int y = lo.y; y <= hi.y; ++y)
-            for (int x = lo.x; x <= hi.x; ++x) {
-                const long long ci = (long long)g.nx * g.ny * z + (long long)g.nx * y + x;
-                const float d = signed_dist_triangle(sdf_cell_pos(g, x, y, z), tri0, tri1, tri2);
-                atomicMin(sdf + ci, float_flip3(d));
-            }
+    const int warpsTotal = gridDim.x * (blockDim.x >> 5);
+    const int lane = threadIdx.x & 31;
+    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < ntri; t += warpsTotal) {
+        const float3 x0 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 0)));
+        const float3 x1 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 1)));
+        const float3 x2 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 2)));
+        sdf_construct_triangle_warp(sdf, g, x0, x1, x2, lane);
+    }
 }
 
 // FinalizeSignedDistanceField, :400-412 (vectorised)
@@ -155,7 +146,8 @@ cudaError_t launch_sdf_initialize(uint32_t* sdf, int64_t cells, cudaStream_t s) 
 cudaError_t launch_sdf_construct(uint32_t* sdf, const SdfGrid& g, const float4* mesh, const uint32_t* idx, int ntri,
                                  cudaStream_t s) {
     if (ntri <= 0) return cudaSuccess;
-    k_sdf_construct<<<(ntri + 127) / 128, 128, 0, s>>>(sdf, g, mesh, idx, ntri);
+    k_sdf_construct<<<(unsigned)std::min<long long>(((long long)ntri + 3) / 4, 152LL * 64), 128, 0, s>>>(sdf, g, mesh,
+                                                                                                 idx, ntri);
     return cudaGetLastError();
 }
 

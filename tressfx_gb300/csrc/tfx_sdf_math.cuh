@@ -38,49 +38,10 @@ __device__ __forceinline__ float3 sdf_cell_pos(const SdfGrid& g, int x, int y, i
     return add(c, mk3(g.ox, g.oy, g.oz));
 }
 
-// DistancePointToEdge, :147-159 (only the distance reaches the result)
-__device__ __forceinline__ float dist_point_edge(float3 p, float3 x0, float3 x1) {
-    const float3 x10 = sub(x1, x0);
-    float t = dot(sub(x1, p), x10) / dot(x10, x10);
-    t = fmaxf(0.0f, fminf(t, 1.0f));
-    const float3 a = sub(p, add(mul(t, x0), mul(1.0f - t, x1)));
-    return length(a);
-}
-
-// SignedDistancePointToTriangle, :163-215
-__device__ __forceinline__ float signed_dist_triangle(float3 p, float3 x0, float3 x1, float3 x2) {
-    float d;
-    float3 x02 = sub(x0, x2);
-    const float l0 = length(x02) + 1e-30f;
-    x02 = divs(x02, l0);
-    float3 x12 = sub(x1, x2);
-    const float l1 = dot(x12, x02);
-    x12 = sub(x12, mul(l1, x02));
-    const float l2 = length(x12) + 1e-30f;
-    x12 = divs(x12, l2);
-    const float3 px2 = sub(p, x2);
-    const float b = dot(x12, px2) / l2;
-    const float a = (dot(x02, px2) - l1 * b) / l0;
-    const float c = (1.0f - a) - b;
-    const float3 nTri = cross(sub(x1, x0), sub(x2, x0));
-    const float tol = 1e-8f;
-    if (a >= -tol && b >= -tol && c >= -tol) {
-        const float3 nn = sub(p, add(add(mul(a, x0), mul(b, x1)), mul(c, x2)));
-        d = length(nn);
-    } else {
-        d = dist_point_edge(p, x0, x1);
-        const float d12 = dist_point_edge(p, x1, x2);
-        const float d02 = dist_point_edge(p, x0, x2);
-        d = fminf(d, d12);
-        d = fminf(d, d02);
-    }
-    d = (dot(sub(p, x0), nTri) < 0.0f) ? -d : d;
-    return d;
-}
-
-// The triangle-only terms of SignedDistancePointToTriangle / DistancePointToEdge, computed once per
-// triangle; signed_dist_pre(p, T) then does the per-cell part.  Every term is the same expression
-// on the same inputs as in signed_dist_triangle, so the distance is bit-identical.
+// SignedDistancePointToTriangle (:163-215) and DistancePointToEdge (:147-159) split in two: the
+// triangle-only terms, computed once per triangle, and signed_dist_pre(p, T), the per-cell part.
+// Every term is the shader's expression on the same inputs in the same order, so the distance is
+// bit-identical to evaluating the two functions per cell.
 struct TriPre {
     float3 x0, x1, x2;
     float3 x02n, x12n;   // normalised edge frame
@@ -151,6 +112,38 @@ __device__ __forceinline__ void tri_cell_box(const SdfGrid& g, float3 t0, float3
     hi = sdf_coords(g, aabbMax);
     lo.x = max(0, min(lo.x - 1, g.nx - 1)); lo.y = max(0, min(lo.y - 1, g.ny - 1)); lo.z = max(0, min(lo.z - 1, g.nz - 1));
     hi.x = max(0, min(hi.x + 1, g.nx - 1)); hi.y = max(0, min(hi.y + 1, g.ny - 1)); hi.z = max(0, min(hi.z + 1, g.nz - 1));
+}
+
+// ConstructSignedDistanceField (:329-397) for one triangle by one warp: the triangle's invariants once,
+// then the lanes over the reference's cell box, each with the same atomicMin on the FloatFlip3 word.
+// Box coordinates of cell c: (c + 0.5) / m lies at least 0.5 / m from an integer, and the float product
+// (c + 0.5) * (1 / m) is within (c / m) * 2^-23 of it, so its truncation is the integer quotient while
+// c < 2^22; larger boxes use integer division.
+__device__ __forceinline__ void sdf_construct_triangle_warp(uint32_t* __restrict__ words, const SdfGrid& g, float3 x0,
+                                                           float3 x1, float3 x2, int lane) {
+    int3 lo, hi;
+    tri_cell_box(g, x0, x1, x2, lo, hi);
+    const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
+    const int nxy = nx * ny;
+    const int vol = nxy * nz;
+    const TriPre P = tri_pre(x0, x1, x2);
+    const bool floatIdx = vol < (1 << 22);
+    const float inxy = 1.0f / (float)nxy, inx = 1.0f / (float)nx;
+    for (int c = lane; c < vol; c += 32) {
+        int cz, r, cy;
+        if (floatIdx) {
+            cz = (int)(((float)c + 0.5f) * inxy);
+            r = c - cz * nxy;
+            cy = (int)(((float)r + 0.5f) * inx);
+        } else {
+            cz = c / nxy;
+            r = c - cz * nxy;
+            cy = r / nx;
+        }
+        const int x = lo.x + (r - cy * nx), y = lo.y + cy, z = lo.z + cz;
+        const float d = signed_dist_pre(sdf_cell_pos(g, x, y, z), P);
+        atomicMin(words + ((long long)z * g.ny + y) * g.nx + x, float_flip3(d));
+    }
 }
 
 // GetSignedDistance + TrilinearInterpolate, :414-527
