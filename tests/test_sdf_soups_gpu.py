@@ -1,0 +1,100 @@
+"""The SDF build on meshes that are not smooth closed surfaces: random triangle soups, the same far from
+the origin, slivers, duplicated and coplanar overlapping triangles (ties of the atomicMin), tiny
+triangles, and a fine grid over a dense mesh -- each grid bit for bit against the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+
+
+def _grid(lo, cell, dims):
+    from tressfx_gb300 import _capi as A
+    g = A.SdfGrid()
+    for k in range(3):
+        g.origin[k] = float(lo[k])
+    g.cell_size = float(cell)
+    g.num_cells_x, g.num_cells_y, g.num_cells_z = dims
+    return g
+
+
+def _soup(kind, rng):
+    n = 600
+    if kind in ("random", "far"):
+        a = rng.uniform(-0.1, 0.1, (n, 3))
+        tri = a[:, None, :] + rng.normal(0, 0.02, (n, 3, 3))
+        if kind == "far":
+            tri += np.array([50.0, -30.0, 20.0])
+    elif kind == "sliver":
+        a = rng.uniform(-0.1, 0.1, (n, 3))
+        d = rng.normal(0, 0.03, (n, 3))
+        t = rng.uniform(0, 1, n)
+        third = a + t[:, None] * d + rng.normal(0, 1e-7, (n, 3))   # almost on the first edge
+        tri = np.stack([a, a + d, third], 1)
+    elif kind == "ties":
+        a = rng.uniform(-0.1, 0.1, (n // 3, 3))
+        base = a[:, None, :] + rng.normal(0, 0.02, (n // 3, 3, 3))
+        shifted = base.copy()
+        shifted[:, 2] = base[:, 0] + 0.5 * (base[:, 2] - base[:, 0])   # coplanar, overlapping
+        tri = np.concatenate([base, base, shifted])                     # exact duplicates too
+    elif kind == "tiny":
+        a = rng.uniform(-0.1, 0.1, (n, 3))
+        tri = a[:, None, :] + rng.normal(0, 1e-4, (n, 3, 3))
+    else:
+        raise ValueError(kind)
+    tri = tri.astype(np.float32)
+    verts = np.zeros((3 * len(tri), 8), np.float32)
+    verts[:, :3] = tri.reshape(-1, 3)
+    return verts, np.arange(3 * len(tri), dtype=np.uint32).reshape(-1, 3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["random", "far", "sliver", "ties", "tiny"])
+def test_construct_on_triangle_soups(ctx, kind):
+    torch = pytest.importorskip("torch")
+    from tressfx_gb300.api import SDFCollision
+    rng = np.random.default_rng({"random": 1, "far": 2, "sliver": 3, "ties": 4, "tiny": 5}[kind])
+    verts, idx = _soup(kind, rng)
+    p = verts[:, :3]
+    lo = p.min(0) - 0.02
+    cell = np.float32((p.max(0) - p.min(0)).max() / 40.0)
+    dims = tuple(int(x) for x in np.ceil((p.max(0) + 0.02 - lo) / cell) + 1)
+    g = _grid(lo, cell, dims)
+    cells = dims[0] * dims[1] * dims[2]
+    dv = torch.from_numpy(verts.reshape(-1)).cuda()
+    di = torch.from_numpy(idx.view(np.int32).reshape(-1)).cuda()
+    sdf = SDFCollision(ctx, cells)
+    try:
+        sdf.set_mesh_device(dv.data_ptr(), len(verts), di.data_ptr(), len(idx))
+        torch.cuda.synchronize()
+        sdf.update(g)
+        got = sdf.read(cells)
+        want = oracle.sdf_build(g, verts, idx.reshape(-1))
+        assert np.array_equal(got, want), f"{int((got != want).sum())} of {cells} cells differ"
+    finally:
+        sdf.close()
+
+
+@pytest.mark.gpu
+def test_construct_fine_grid_dense_mesh(ctx):
+    torch = pytest.importorskip("torch")
+    from tressfx_gb300.api import SDFCollision
+    from tressfx_gb300.synthetic import head_mesh
+    m = head_mesh(30000)
+    verts = np.ascontiguousarray(m.vertices, np.float32).reshape(-1, 8)
+    idx = np.ascontiguousarray(m.indices, np.uint32).reshape(-1, 3)
+    p = verts[:, :3]
+    lo = p.min(0) - 0.01
+    cell = np.float32((p.max(0) - p.min(0)).max() / 110.0)
+    dims = tuple(int(x) for x in np.ceil((p.max(0) + 0.01 - lo) / cell) + 1)
+    g = _grid(lo, cell, dims)
+    cells = dims[0] * dims[1] * dims[2]
+    dv = torch.from_numpy(verts.reshape(-1)).cuda()
+    di = torch.from_numpy(idx.view(np.int32).reshape(-1)).cuda()
+    sdf = SDFCollision(ctx, cells)
+    try:
+        sdf.set_mesh_device(dv.data_ptr(), len(verts), di.data_ptr(), len(idx))
+        torch.cuda.synchronize()
+        sdf.update(g)
+        assert np.array_equal(sdf.read(cells), oracle.sdf_build(g, verts, idx.reshape(-1)))
+    finally:
+        sdf.close()
