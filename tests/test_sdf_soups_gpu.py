@@ -1,6 +1,7 @@
 """The SDF build on meshes that are not smooth closed surfaces: random triangle soups, the same far from
 the origin, slivers, duplicated and coplanar overlapping triangles (ties of the atomicMin), tiny
-triangles, and a fine grid over a dense mesh -- each grid bit for bit against the oracle."""
+triangles, a fine grid over a dense mesh, and Construct alone on words already near its result --
+each grid bit for bit against the oracle."""
 import numpy as np
 import pytest
 
@@ -96,5 +97,56 @@ def test_construct_fine_grid_dense_mesh(ctx):
         torch.cuda.synchronize()
         sdf.update(g)
         assert np.array_equal(sdf.read(cells), oracle.sdf_build(g, verts, idx.reshape(-1)))
+    finally:
+        sdf.close()
+
+
+def _flip(f32: np.ndarray) -> np.ndarray:
+    u = f32.view(np.uint32)
+    return ((u << np.uint32(1)) | (u >> np.uint32(31))).astype(np.uint32)
+
+
+def _unflip(w: np.ndarray) -> np.ndarray:
+    return ((w >> np.uint32(1)) | (w << np.uint32(31))).astype(np.uint32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["random", "ties", "tiny", "far"])
+def test_construct_from_words_near_its_result(ctx, kind):
+    """Construct alone on words that already sit within a few ulps of the result, with either sign:
+    every pair's word lies close to a cell's current word, the case in which skipping pairs that
+    cannot lower a word is hardest to get right.  The grid must still be the reference's
+    atomicMin of every pair into those words."""
+    torch = pytest.importorskip("torch")
+    from tressfx_gb300 import _capi as A
+    from tressfx_gb300.api import SDFCollision
+    rng = np.random.default_rng({"random": 11, "ties": 12, "tiny": 13, "far": 14}[kind])
+    verts, idx = _soup(kind, rng)
+    p = verts[:, :3]
+    lo = p.min(0) - 0.02
+    cell = np.float32((p.max(0) - p.min(0)).max() / 40.0)
+    dims = tuple(int(x) for x in np.ceil((p.max(0) + 0.02 - lo) / cell) + 1)
+    g = _grid(lo, cell, dims)
+    cells = dims[0] * dims[1] * dims[2]
+    result = _flip(np.full(cells, 1e10, np.float32))
+    oracle.sdf_construct(g, result, verts, idx.reshape(-1))
+    mag = _unflip(result) & np.uint32(0x7FFFFFFF)
+    step = rng.integers(-3, 4, cells)
+    mag = np.clip(mag.astype(np.int64) + step, 0, 0x7F7FFFFF).astype(np.uint32)
+    sign = rng.integers(0, 2, cells).astype(np.uint32) << np.uint32(31)
+    start = _flip((mag | sign).view(np.float32))
+    want = start.copy()
+    oracle.sdf_construct(g, want, verts, idx.reshape(-1))
+    assert int((want != start).sum()) > 0
+    dv = torch.from_numpy(verts.reshape(-1)).cuda()
+    di = torch.from_numpy(idx.view(np.int32).reshape(-1)).cuda()
+    sdf = SDFCollision(ctx, cells)
+    try:
+        sdf.set_mesh_device(dv.data_ptr(), len(verts), di.data_ptr(), len(idx))
+        sdf.write(start)
+        torch.cuda.synchronize()
+        sdf.dispatch(A.K_SDF_CONSTRUCT, g)
+        got = sdf.read(cells)
+        assert np.array_equal(got, want), f"{int((got != want).sum())} of {cells} cells differ"
     finally:
         sdf.close()
