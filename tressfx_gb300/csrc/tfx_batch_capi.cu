@@ -482,6 +482,17 @@ static int autotune(tfx_batch b, int frames) {
                 if (rc) break;
             }
         }
+        // Fewer resident strand blocks leave room on each SM for the concurrent SDF construct's
+        // blocks: two lower caps for the best shape.
+        const int perSM = fused_blocks_per_sm(c.n, bestV, bestW);
+        const int from = (bestCap > 0 ? bestCap : perSM - 1) - 1;   // the loop above tried perSM and perSM - 1
+        for (int cap = from; rc == TFX_OK && cap >= std::max(1, from - 1); --cap) {
+            c.splitSweeps = bestSplit; c.vpl = bestV; c.warps = bestW; c.perSMCap = cap;
+            if ((rc = size_class(b, c))) break;
+            float ms;
+            if ((rc = time_graph_frames(b, frames, &ms))) break;
+            if (ms < best) { best = ms; bestCap = cap; }
+        }
         c.vpl = bestV; c.warps = bestW; c.perSMCap = bestCap; c.splitSweeps = bestSplit;
         if (rc == TFX_OK) rc = size_class(b, c);
     }

@@ -15,8 +15,8 @@
 //  * k_fused_strands      - the six simulation stages of the guide strands (TressFXSimulation.hlsl:
 //                           609-975) for a group of guide strands (32, or 16 at n = 64) in one
 //                           pass.  Phase 0: bulk asynchronous copies (cp.async.bulk on an mbarrier)
-//                           bring the group's Pos / Prev / InitialPos / Tangent / RestLength rows into
-//                           shared memory while warp 0 blends each strand's bone matrix.  Phase 1a
+//                           bring the group's Pos and InitialPos rows into shared memory while warp 0
+//                           blends each strand's bone matrix.  Phase 1a
 //                           (one lane per strand): strand-level data.  Phase 1b (one thread per
 //                           vertex): integration + global shape, VSP, bind pose.  Phase 2 (one lane
 //                           per strand, one warp per iteration): the local-shape sweeps as a
@@ -160,15 +160,15 @@ __global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __r
 // One block runs one group of GS = fused_group_strands(N) guide strands of one object at a time.
 // Shared memory, strand-major rows of N vertices padded to N+1 float4, so that both the one-lane-per-
 // strand sweep and the one-lane-per-vertex passes are free of bank conflicts:
-//   TP[GS][N+1] positions   TI[GS][N+1] InitialPos, then the bind pose   TR[GS][N] rest lengths
+//   TP[GS][N+1] positions   TI[GS][N+1] InitialPos, then the bind pose
 //   SK[GS][4] blended bone matrix rows   SL[GS][3] StrandLevelData
 //   one mbarrier, on which the bulk copies that bring a group's rows in complete.
-// Prev and Tangent never enter shared memory: each thread reads and writes its own vertices' words
-// in global memory (coalesced), which keeps a block small enough for five to fit per SM, and the
-// serial local-shape sweeps of that many groups to run side by side.
+// Prev, Tangent and RestLength never enter shared memory: each thread reads (and writes) its own
+// vertices' words in global memory (coalesced), which keeps a block small enough for six to fit per
+// SM at n = 32 and 64, and the serial local-shape sweeps of that many groups to run side by side.
 __host__ __device__ constexpr int fused_group_strands(int n) { return n >= 64 ? 16 : 32; }
 __host__ __device__ constexpr int fused_smem_for(int n) {
-    return 2 * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * n * 4 + fused_group_strands(n) * 7 * 16 + 16;
+    return 2 * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * 7 * 16 + 16;
 }
 constexpr int kFusedWaitPolls = 1 << 21;
 // k_fused_strands modes: the whole frame of the group, or its part before the local-shape sweeps
@@ -274,8 +274,7 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
     extern __shared__ float4 smem_f4[];
     float4* TP = smem_f4;
     float4* TI = TP + GS * RS;
-    float* TR = reinterpret_cast<float*>(TI + GS * RS);
-    float4* SK = reinterpret_cast<float4*>(TR + GS * N);
+    float4* SK = TI + GS * RS;
     float4* SL = SK + GS * 4;
     const uint32_t bar = smem_u32(SL + GS * 3);
 
@@ -302,15 +301,14 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
         float4 bq4 = make_float4(0.f, 0.f, 0.f, 0.f);
         const bool pre = mode != kFusedPost, post = mode != kFusedPre;   // phases 0-2 / phase 3 run
         if (warp == 0) {
-            // rows: Pos always; InitialPos for phases 0-2; RestLength for phase 3
-            const uint32_t rowBytes = N * 16 + (pre ? N * 16 : 0) + (post ? N * 4 : 0);
+            // rows: Pos always; InitialPos for phases 0-2
+            const uint32_t rowBytes = N * 16 + (pre ? N * 16 : 0);
             if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)count * rowBytes);
             __syncwarp();
             if (lane < count) {
                 const size_t vo = (size_t)(gs0 + lane * (F + 1)) * N;
                 bulk_g2s(smem_u32(TP + lane * RS), h.pos + vo, N * 16, bar);
                 if (pre) bulk_g2s(smem_u32(TI + lane * RS), h.init + vo, N * 16, bar);
-                if (post) bulk_g2s(smem_u32(TR + lane * N), h.rest + vo, N * 4, bar);
             }
             if (pre && lane < count) {
                 // strand level, while the rows are in flight: the blended bone matrix and its quaternion
@@ -436,7 +434,7 @@ __global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const B
                     p[k] = TP[base + k];
                     pv[k] = h.prev[vrow + q * VPL + k];
                     tn[k] = h.tan[vrow + q * VPL + k];
-                    len[k] = TR[s * N + q * VPL + k];
+                    len[k] = __ldg(h.rest + vrow + q * VPL + k);
                 } else {
                     p[k] = pv[k] = tn[k] = make_float4(0.f, 0.f, 0.f, 0.f);
                     len[k] = 0.0f;
