@@ -263,8 +263,10 @@ __device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const f
     }
 }
 
+// Register bounds: at n <= 16 the tiles are small (21 KB a block) and registers decide residency, so
+// 64 a thread (eight 4-warp blocks per SM; a few words spill) beat 80 (six blocks).
 template <int N, int VPL>
-__global__ void __launch_bounds__(256, VPL <= 2 ? 3 : 2) k_fused_strands(const BatchObject* __restrict__ objs,
+__global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused_strands(const BatchObject* __restrict__ objs,
                                                                         const WorkItem* __restrict__ items, int numItems,
                                                                         int* err, int mode) {
     constexpr int GS = fused_group_strands(N);
