@@ -14,7 +14,8 @@ synthetic):
 value  = vertices simulated per second over exactly --steps timed frames of the batched path (one
          CUDA-graph launch per frame), device time from CUDA events on the library's stream, inputs
          resident in HBM.  The plain path (one launch per object per stage, the reference's dispatch
-         structure) is timed the same way and reported under "plain".
+         structure) is timed the same way and reported under "plain".  "guide_value" counts the
+         guide vertices only (follow hairs are generated, not simulated).
 e2e    = the same metric through the public C ABI with host buffers: every frame uploads its inputs
          (constants, bone matrices, grids) from pinned memory and delivers all simulated positions
          (x, y, z; the inverse mass w never changes) into pinned memory (tfx_batch_readback: a device
@@ -638,6 +639,15 @@ def main() -> None:
         el, fr = oracle_sample(scene, args.cpu_seconds, 4 * args.cpu_seconds, threads)
         cpu = {"value": scene.vertices_per_frame * fr / el, "unit": "vertex-steps/s", "cores": threads, "kind": "port",
                "sample": f"{fr} full frames of the workload after one untimed frame ({el:.1f} s, oracle restatement)"}
+        one_core = el / fr * threads   # estimated seconds per frame on one core
+        if one_core <= args.cpu_seconds:
+            el1, fr1 = oracle_sample(scene, min(args.cpu_seconds / 4, 2 * one_core), args.cpu_seconds, 1)
+            cpu["single_thread_value"] = scene.vertices_per_frame * fr1 / el1
+            cpu["single_thread_sample"] = f"{fr1} full frames on one thread ({el1:.1f} s)"
+        else:
+            cpu["single_thread_value"] = None
+            cpu["single_thread_sample"] = f"not sampled: one frame takes about {one_core:.0f} s on one thread"
+        guide_vpf = sum(o.asset.num_guide_strands * o.asset.verts_per_strand for o in scene.objects)
         peaks = load_peaks()
         sb, fbw = strand_bytes(scene), follow_bytes(scene)
         classes = sorted(sb)
@@ -656,6 +666,7 @@ def main() -> None:
         achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
         line = {
             "metric": metric, "value": value, "unit": "vertex-steps/s", "n_gpus": world, "steps": args.steps,
+            "guide_value": guide_vpf * world / (ms * 1e-3),
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": dict(base_cfg, path="batched: one CUDA graph per frame (mesh skinning + SDF build on one "
