@@ -581,7 +581,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--autotune", type=int, default=2, help="frames per candidate shape (0: defaults)")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--nsdf-steps", type=int, default=6000, help="training steps of the proxy (--config neural)")
+    ap.add_argument("--nsdf-steps", type=int, default=24000, help="training steps of the proxy (--config neural)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
