@@ -4,7 +4,7 @@ Every kernel is compared from identical state (stage by stage), then whole frame
 over many frames, over every legal vertices-per-strand count, with follow hairs, wind, SDF
 collision, reset frames, ragged strand counts and the full benchmark sizes.  The tolerance is
 exact equality of the float32 bit patterns (no FMA contraction, IEEE division and square root on
-both sides); the benchmark spec's bound of 1e-5 x strand length is reported alongside.
+both sides); the 1e-5 x strand-length position bound is reported alongside.
 """
 import numpy as np
 import pytest
@@ -193,7 +193,7 @@ def test_sdf_reference_grid_rule_bit_exact(ctx):
 
 @pytest.mark.parametrize("which", ["head", "fur"])
 def test_full_size_first_frames_bit_exact(ctx, which):
-    """BASELINE-size workloads (20k x 32 x 5 with SDF 64^3; 200k x 16 with SDF 128^3): two frames."""
+    """Full-size workloads (20k x 32 x 5 with SDF 64^3; 200k x 16 with SDF 128^3): two frames."""
     sc = scene_head() if which == "head" else scene_fur()
     gpu = PlainPipeline(ctx, sc)
     ora = OraclePipeline(sc)
