@@ -242,6 +242,23 @@ __device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const f
     constexpr int RS = N + 1;
     float4* P = SP + s * RS;
     const float4* B = SB + s * RS;
+    if (KW == 1) {
+        // A single sweep: no other warp reads this warp's stores, so the steps need no barrier, and
+        // row element j + 2 (read once, at step j + 1, and written only after that) loads a step early.
+        if (!active) return;
+        float4 pm1 = P[0], pos = P[1], next = P[2];
+        float3 bm1 = xyz(B[0]), b0 = xyz(B[1]), bnext = xyz(B[2]);
+        for (int j = 1; j <= N - 2; ++j) {
+            float4 pp1 = next;
+            const float3 bp1 = bnext;
+            if (j + 2 <= N - 1) { next = P[j + 2]; bnext = xyz(B[j + 2]); }
+            local_shape_step(pm1, pos, pp1, bm1, b0, bp1, stiff);
+            P[j] = pos;
+            pm1 = pos; pos = pp1; bm1 = b0; b0 = bp1;
+        }
+        P[N - 1] = pos;
+        return;
+    }
     float4 pm1 = make_float4(0.f, 0.f, 0.f, 0.f), pos = pm1;
     float3 bm1 = mk3(0.f, 0.f, 0.f), b0 = bm1;
     const int T = (N - 2) + 2 * (KW - 1);
