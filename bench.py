@@ -131,10 +131,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_scene(name: str):
+def make_scene(name: str, objects: int = 64):
     from tressfx_gb300 import synthetic as S
-    return {"head": S.scene_head, "fur": S.scene_fur, "small": S.scene_small, "batched": S.scene_batched,
-            "neural": S.scene_neural}[name]()
+    if name == "batched":
+        return S.scene_batched(num_objects=objects)
+    return {"head": S.scene_head, "fur": S.scene_fur, "small": S.scene_small, "neural": S.scene_neural}[name]()
 
 
 def plain_kernel_bytes(scene) -> dict[str, float]:
@@ -353,7 +354,7 @@ def oracle_sample(scene, min_seconds: float, max_seconds: float, threads: int) -
 
 
 def run_reference(args) -> dict:
-    scene = make_scene(args.config)
+    scene = make_scene(args.config, args.objects)
     threads = os.cpu_count() or 1
     from oracle.scene_driver import OraclePipeline
     from tressfx_gb300.headless import FrameInputs
@@ -581,6 +582,8 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--autotune", type=int, default=2, help="frames per candidate shape (0: defaults)")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--objects", type=int, default=64,
+                    help="--config batched: the first N objects of its seeded draw (a small case for profiling)")
     ap.add_argument("--nsdf-steps", type=int, default=24000, help="training steps of the proxy (--config neural)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -593,7 +596,10 @@ def main() -> None:
         import torch.distributed as dist
         dist.init_process_group("gloo")
     metric = "hair vertex-steps/s"
-    base_cfg = {"workload": WORKLOADS[args.config], "parallelism": f"{world} replicas" if world > 1 else "single GPU",
+    workload = WORKLOADS[args.config]
+    if args.config == "batched" and args.objects != 64:
+        workload = f"the first {args.objects} objects of: {workload}"
+    base_cfg = {"workload": workload, "parallelism": f"{world} replicas" if world > 1 else "single GPU",
                 "l2": "inputs larger than L2 (state of 3.2M+ vertices >= 256 MB per frame)"}
 
     if args.impl == "reference":
@@ -622,7 +628,7 @@ def main() -> None:
         return
 
     from tressfx_gb300.api import Context
-    scene = make_scene(args.config)
+    scene = make_scene(args.config, args.objects)
     ctx = Context(local)
     b = run_batched(ctx, scene, args.steps, args.warmup, local, args.autotune)
     p = None if args.no_plain else run_plain(ctx, scene, min(args.steps, 100), args.warmup)
