@@ -34,6 +34,7 @@ struct BatchClass {
     int perSMCap = 0;            // resident strand blocks per SM allowed (0 = as many as fit)
     int followBlocks = 1;        // grid of k_follow_collide (persistent over the chunks)
     int followChunks = 1;        // chunks per group in k_follow_collide
+    bool followQueued = false;   // k_follow_collide_queued: some object of the class has follow hairs
     bool splitSweeps = false;    // local-shape sweeps in k_local_sweep between two strand passes
     std::vector<WorkItem> hostItems;
     WorkItem* items = nullptr;  // device
@@ -187,9 +188,10 @@ static void describe(tfx_batch b) {
     char buf[1024];
     int k = snprintf(buf, sizeof(buf), "sdf construct %d threads/block;", b->sdfL.constructThreads);
     for (auto& c : b->classes)
-        k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d%s;",
+        k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d%s%s;",
                       c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n),
-                      c.splitSweeps ? ", sweeps in their own launch" : "");
+                      c.splitSweeps ? ", sweeps in their own launch" : "",
+                      c.followQueued ? ", collide on per-warp lookup queues" : "");
     k += snprintf(buf + k, sizeof(buf) - k, " SDF build %s the strand kernels%s;",
                   b->overlap ? "concurrent with" : "before", b->sdfL.expand ? ", lookups on corner-expanded grids" : "");
     b->description = buf;
@@ -197,9 +199,11 @@ static void describe(tfx_batch b) {
 
 static void make_items(tfx_batch b, BatchClass& c) {
     c.hostItems.clear();
+    c.followQueued = false;
     for (int o = 0; o < (int)b->hairs.size(); ++o) {
         tfx_hair h = b->hairs[o];
         if (h->n != c.n) continue;
+        c.followQueued |= h->F > 0;
         const int gsz = fused_group_size(c.n);
         for (int g = 0; g < h->G; g += gsz) c.hostItems.push_back(WorkItem{o, g, std::min(gsz, h->G - g), 0});
     }
@@ -223,7 +227,7 @@ static int size_class(tfx_batch b, BatchClass& c) {
     if (c.perSMCap > 0) perSM = std::min(perSM, c.perSMCap);
     c.blocks = std::max(1, std::min(perSM * b->ctx->numSMs, c.numItems));
     // follow/collide: whole groups when every resident block gets at least four, else the smallest chunks
-    const int fResident = std::max(1, follow_blocks_per_sm(c.n)) * b->ctx->numSMs;
+    const int fResident = std::max(1, follow_blocks_per_sm(c.n, c.followQueued)) * b->ctx->numSMs;
     c.followChunks = c.numItems >= 4 * fResident ? 1 : follow_max_chunks_per_item(c.n);
     c.followBlocks = std::max(1, std::min(fResident, c.numItems * c.followChunks));
     return TFX_OK;
@@ -257,7 +261,7 @@ static int launch_strands(tfx_batch b, BatchClass& c, cudaStream_t s) {
 }
 
 static int launch_follows(tfx_batch b, BatchClass& c, cudaStream_t s) {
-    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems, c.followChunks};
+    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems, c.followChunks, c.followQueued ? 1 : 0};
     cudaError_t e = launch_follow_collide(fl, s);
     return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: follow/collide launch");
 }

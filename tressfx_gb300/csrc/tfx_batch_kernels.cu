@@ -815,6 +815,132 @@ __global__ void __launch_bounds__(256, 4) k_follow_collide(const BatchObject* __
 }
 
 // ============================================================================================
+// follow hairs + collision with per-warp lookup queues (classes whose objects have follow hairs)
+//
+// The same work as k_follow_collide, with the warp's lanes decoupled from its lookups: lane l owns one
+// guide vertex, makes and writes its follow vertices, and queues every vertex (guide or follow) the
+// collision may move (j >= 2, not certainly outside the grid).  The warp runs the first lookup on 32
+// queued vertices at a time, then the gradient stage on 32 of those within the margin at a time, so
+// both run on full warps: a strand reaches from the scalp, where vertices touch the surface, out to
+// tips far from it, and with follow hairs a lane has F + 1 vertices of that mix.  A moved vertex gets
+// Pos and Prev from the lane that collided it, after the owner's write of the follow's Pos
+// (__syncwarp orders the two).  The queues are emptied at the end of each chunk.
+constexpr int kFollowWarps = 8;
+struct FollowQueues {
+    int idx1[kFollowWarps][64];      // stage 1: offset of the vertex in the group
+    float4 pos1[kFollowWarps][64];   //          its position and inverse mass
+    int idx2[kFollowWarps][64];      // stage 2: the same, for vertices within the margin
+    float4 pos2[kFollowWarps][64];
+    float dist2[kFollowWarps][64];   //          and their first lookup's distance
+};
+
+// Lane k < n takes entry k of a queue; the entries from 32 on move to the front.
+__device__ __forceinline__ bool queue_take(int* idx, float4* pos, float* dist, int& n, int lane, int& ri, float4& rp,
+                                           float& rd) {
+    __syncwarp();
+    const bool have = lane < n;
+    if (have) { ri = idx[lane]; rp = pos[lane]; if (dist) rd = dist[lane]; }
+    __syncwarp();
+    if (lane < n - 32) { idx[lane] = idx[lane + 32]; pos[lane] = pos[lane + 32]; if (dist) dist[lane] = dist[lane + 32]; }
+    __syncwarp();
+    n = max(n - 32, 0);
+    return have;
+}
+
+// Stage 2 on up to 32 queued vertices: the gradient lookups and, inside the margin, the projection.
+__device__ __forceinline__ void follow_stage2(const FollowGroup& fg, size_t vbase, FollowQueues& Q, int warp, int lane,
+                                              int& n2) {
+    int ri = 0; float4 rp = make_float4(0.f, 0.f, 0.f, 0.f); float rd = 0.0f;
+    if (!queue_take(Q.idx2[warp], Q.pos2[warp], Q.dist2[warp], n2, lane, ri, rp, rd)) return;
+    float3 proj;
+    if (collide_near(fg.sdf, fg.sdf8, fg.sg, fg.margin, xyz(rp), rd, &proj)) {
+        const size_t v = vbase + (size_t)ri;
+        fg.h.pos[v] = make_float4(proj.x, proj.y, proj.z, rp.w);
+        fg.h.prev[v] = with_xyz(fg.h.prev[v], proj);
+    }
+}
+
+// Stage 1 on up to 32 queued vertices: the first lookup; those within the margin join stage 2.
+__device__ __forceinline__ void follow_stage1(const FollowGroup& fg, size_t vbase, FollowQueues& Q, int warp, int lane,
+                                              int& n1, int& n2) {
+    int ri = 0; float4 rp = make_float4(0.f, 0.f, 0.f, 0.f); float rd = 0.0f;
+    const bool have = queue_take(Q.idx1[warp], Q.pos1[warp], nullptr, n1, lane, ri, rp, rd);
+    bool near = false;
+    if (have) {
+        rd = fg.sdf8 ? sdf_lookup8(fg.sdf8, fg.sg, xyz(rp)) : sdf_lookup(fg.sdf, fg.sg, xyz(rp));
+        near = rd <= fg.margin;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, near);
+    if (near) {
+        const int k = n2 + __popc(m & ((1u << lane) - 1u));
+        Q.idx2[warp][k] = ri; Q.pos2[warp][k] = rp; Q.dist2[warp][k] = rd;
+    }
+    n2 += __popc(m);
+    if (n2 >= 32) follow_stage2(fg, vbase, Q, warp, lane, n2);
+}
+
+template <int N>
+__global__ void __launch_bounds__(256, 4) k_follow_collide_queued(const BatchObject* __restrict__ objs,
+                                                                  const WorkItem* __restrict__ items, int numItems,
+                                                                  int chunksPerItem) {
+    constexpr int kGroupVerts = fused_group_strands(N) * N;
+    constexpr float kInvN = 1.0f / (float)N;   // exact: N is a power of two, so j * kInvN == j / N
+    __shared__ FollowQueues Q;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const int chunkLen = ((kGroupVerts + chunksPerItem - 1) / chunksPerItem + 255) & ~255;
+    const int numChunks = numItems * chunksPerItem;
+    for (int c = blockIdx.x; c < numChunks; c += gridDim.x) {
+        const int it = c / chunksPerItem;
+        const WorkItem wi = items[it];
+        const int begin = (c - it * chunksPerItem) * chunkLen;
+        const int end = min(begin + chunkLen, wi.count * N);
+        FollowGroup fg;
+        if (!follow_group(objs[wi.obj], wi, fg)) continue;
+        const HairView& h = fg.h;
+        const int F = h.F;
+        const size_t vbase = (size_t)fg.firstStrand * N;
+        int n1 = 0, n2 = 0;
+        for (int base = begin + warp * 32; base < end; base += blockDim.x) {
+            const int e = base + lane;
+            const bool active = e < end;
+            const int s = e / N, j = e % N;
+            const int gs = fg.firstStrand + s * (F + 1);
+            const size_t vg = (size_t)gs * N + j;
+            float4 gp = make_float4(0.f, 0.f, 0.f, 0.f), tn = gp;
+            if (active) { gp = h.pos[vg]; tn = h.tan[vg]; }
+            const bool collide = active && fg.sdf && j >= 2;
+            const float factor = fg.tip * ((float)j * kInvN) + 1.0f;
+            for (int i = 0; i <= F; ++i) {
+                const size_t v = vg + (size_t)i * N;
+                float3 pt = xyz(gp);
+                float w = gp.w;
+                if (active && i > 0) {
+                    const float4 off = __ldg(h.followOffset + gs + i);
+                    pt = add(xyz(gp), mul(factor, xyz(off)));
+                    // inverse mass of the follow vertex: only this lane writes the word, after this read
+                    w = __ldg(&h.pos[v].w);
+                    h.pos[v] = make_float4(pt.x, pt.y, pt.z, w);
+                    h.tan[v] = tn;
+                }
+                const bool need = collide && !sdf_surely_outside(fg.sg, pt);
+                const unsigned m = __ballot_sync(0xffffffffu, need);
+                if (need) {
+                    const int k = n1 + __popc(m & below);
+                    Q.idx1[warp][k] = (int)(v - vbase);
+                    Q.pos1[warp][k] = make_float4(pt.x, pt.y, pt.z, w);
+                }
+                n1 += __popc(m);
+                if (n1 >= 32) follow_stage1(fg, vbase, Q, warp, lane, n1, n2);
+            }
+        }
+        while (n1 > 0) follow_stage1(fg, vbase, Q, warp, lane, n1, n2);
+        while (n2 > 0) follow_stage2(fg, vbase, Q, warp, lane, n2);
+        __syncwarp();
+    }
+}
+
+// ============================================================================================
 // readback snapshot: every object's positions, one after the other, as float4 (xyzw) or packed xyz
 __global__ void __launch_bounds__(256) k_snapshot_positions(const BatchObject* __restrict__ objs,
                                                             const long long* __restrict__ first, int nobj,
@@ -937,21 +1063,28 @@ int follow_max_chunks_per_item(int n) { return (fused_group_strands(n) * n + 255
 
 template <int N>
 static cudaError_t launch_follow_n(const FollowLaunch& fl, cudaStream_t s) {
-    k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+    if (fl.queued) k_follow_collide_queued<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+    else k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
     return cudaGetLastError();
 }
 
-int follow_blocks_per_sm(int n) {
+int follow_blocks_per_sm(int n, bool queued) {
     int nb = 0;
     cudaError_t e = cudaErrorInvalidValue;
+#define TFX_FOLLOW_OCC(NN)                                                                                      \
+    case NN:                                                                                                    \
+        e = queued ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide_queued<NN>, 256, 0) \
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<NN>, 256, 0);        \
+        break;
     switch (n) {
-        case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<4>, 256, 0); break;
-        case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<8>, 256, 0); break;
-        case 16: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<16>, 256, 0); break;
-        case 32: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<32>, 256, 0); break;
-        case 64: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<64>, 256, 0); break;
+        TFX_FOLLOW_OCC(4)
+        TFX_FOLLOW_OCC(8)
+        TFX_FOLLOW_OCC(16)
+        TFX_FOLLOW_OCC(32)
+        TFX_FOLLOW_OCC(64)
         default: break;
     }
+#undef TFX_FOLLOW_OCC
     return e == cudaSuccess ? nb : 0;
 }
 
