@@ -11,7 +11,8 @@
 // has executed.
 //
 // Autotuning.  tfx_batch_autotune(b, frames) times the candidate launch shapes (vertices per lane
-// and warps per block of every fused class, block size of the SDF construct) on the real objects,
+// and warps per block of every fused class, the form of its follow/collide kernel, block size of the
+// SDF construct) on the real objects,
 // restores every state buffer it touched, and recaptures the graphs with the fastest shape of each
 // part.  All shapes give the same bits; only the speed differs.
 #include <cuda_runtime.h>
@@ -34,7 +35,9 @@ struct BatchClass {
     int perSMCap = 0;            // resident strand blocks per SM allowed (0 = as many as fit)
     int followBlocks = 1;        // grid of k_follow_collide (persistent over the chunks)
     int followChunks = 1;        // chunks per group in k_follow_collide
-    bool followQueued = false;   // k_follow_collide_queued: some object of the class has follow hairs
+    int followMode = 0;          // FollowLaunch::queued.  Default, from measurements: 1 when an object of the
+                                 // class has follow hairs, else 2 at n >= 64 (long strands: lanes of one warp
+                                 // reach both surface and far vertices), else 0; the autotuner tries the others
     bool splitSweeps = false;    // local-shape sweeps in k_local_sweep between two strand passes
     std::vector<WorkItem> hostItems;
     WorkItem* items = nullptr;  // device
@@ -191,7 +194,8 @@ static void describe(tfx_batch b) {
         k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d%s%s;",
                       c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n),
                       c.splitSweeps ? ", sweeps in their own launch" : "",
-                      c.followQueued ? ", collide on per-warp lookup queues" : "");
+                      c.followMode == 1 ? ", collide on per-warp lookup queues"
+                                         : c.followMode == 2 ? ", gradient lookups on per-warp queues" : "");
     k += snprintf(buf + k, sizeof(buf) - k, " SDF build %s the strand kernels%s;",
                   b->overlap ? "concurrent with" : "before", b->sdfL.expand ? ", lookups on corner-expanded grids" : "");
     b->description = buf;
@@ -199,11 +203,11 @@ static void describe(tfx_batch b) {
 
 static void make_items(tfx_batch b, BatchClass& c) {
     c.hostItems.clear();
-    c.followQueued = false;
+    c.followMode = c.n >= 64 ? 2 : 0;
     for (int o = 0; o < (int)b->hairs.size(); ++o) {
         tfx_hair h = b->hairs[o];
         if (h->n != c.n) continue;
-        c.followQueued |= h->F > 0;
+        if (h->F > 0) c.followMode = 1;
         const int gsz = fused_group_size(c.n);
         for (int g = 0; g < h->G; g += gsz) c.hostItems.push_back(WorkItem{o, g, std::min(gsz, h->G - g), 0});
     }
@@ -227,7 +231,7 @@ static int size_class(tfx_batch b, BatchClass& c) {
     if (c.perSMCap > 0) perSM = std::min(perSM, c.perSMCap);
     c.blocks = std::max(1, std::min(perSM * b->ctx->numSMs, c.numItems));
     // follow/collide: whole groups when every resident block gets at least four, else the smallest chunks
-    const int fResident = std::max(1, follow_blocks_per_sm(c.n, c.followQueued)) * b->ctx->numSMs;
+    const int fResident = std::max(1, follow_blocks_per_sm(c.n, c.followMode)) * b->ctx->numSMs;
     c.followChunks = c.numItems >= 4 * fResident ? 1 : follow_max_chunks_per_item(c.n);
     c.followBlocks = std::max(1, std::min(fResident, c.numItems * c.followChunks));
     return TFX_OK;
@@ -261,7 +265,7 @@ static int launch_strands(tfx_batch b, BatchClass& c, cudaStream_t s) {
 }
 
 static int launch_follows(tfx_batch b, BatchClass& c, cudaStream_t s) {
-    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems, c.followChunks, c.followQueued ? 1 : 0};
+    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems, c.followChunks, c.followMode};
     cudaError_t e = launch_follow_collide(fl, s);
     return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: follow/collide launch");
 }
@@ -437,7 +441,8 @@ static int time_graph_frames(tfx_batch b, int frames, float* ms) {
 
 // Coordinate descent over the launch shapes, each candidate timed as whole frames of the graph
 // (the SDF branch overlaps the strand kernels, so a part cannot be timed alone): the SDF construct's
-// block size, then per class the vertices per lane, warps per block and resident blocks per SM.
+// block size, then per class the vertices per lane, warps per block, resident blocks per SM and the
+// form of the follow/collide kernel.
 static int autotune(tfx_batch b, int frames) {
     cudaStream_t s = b->ctx->stream;
     for (int i = 0; i < 2; ++i) std::memcpy(b->pinned[i], b->staging.data(), b->blockBytes);
@@ -498,6 +503,17 @@ static int autotune(tfx_batch b, int frames) {
             if (ms < best) { best = ms; bestCap = cap; }
         }
         c.vpl = bestV; c.warps = bestW; c.perSMCap = bestCap; c.splitSweeps = bestSplit;
+        // the follow/collide form: one vertex at a time, both lookup stages queued, or the gradient stage
+        int bestMode = c.followMode;
+        for (int mode = 0; rc == TFX_OK && mode < 3; ++mode) {
+            if (mode == bestMode) continue;
+            c.followMode = mode;
+            if ((rc = size_class(b, c))) break;
+            float ms;
+            if ((rc = time_graph_frames(b, frames, &ms))) break;
+            if (ms < 0.99f * best) { best = ms; bestMode = mode; }   // a measured default yields to a clear gain only
+        }
+        c.followMode = bestMode;
         if (rc == TFX_OK) rc = size_class(b, c);
     }
     int rr = snapshot_restore(sn, s);

@@ -879,7 +879,9 @@ __device__ __forceinline__ void follow_stage1(const FollowGroup& fg, size_t vbas
     if (n2 >= 32) follow_stage2(fg, vbase, Q, warp, lane, n2);
 }
 
-template <int N>
+// QueueFirst = false: each lane runs its vertices' first lookup itself and only the vertices within
+// the margin are queued (for classes without follow hairs, where a lane has one vertex per step).
+template <int N, bool QueueFirst>
 __global__ void __launch_bounds__(256, 4) k_follow_collide_queued(const BatchObject* __restrict__ objs,
                                                                   const WorkItem* __restrict__ items, int numItems,
                                                                   int chunksPerItem) {
@@ -924,14 +926,29 @@ __global__ void __launch_bounds__(256, 4) k_follow_collide_queued(const BatchObj
                     h.tan[v] = tn;
                 }
                 const bool need = collide && !sdf_surely_outside(fg.sg, pt);
-                const unsigned m = __ballot_sync(0xffffffffu, need);
-                if (need) {
-                    const int k = n1 + __popc(m & below);
-                    Q.idx1[warp][k] = (int)(v - vbase);
-                    Q.pos1[warp][k] = make_float4(pt.x, pt.y, pt.z, w);
+                if (QueueFirst) {
+                    const unsigned m = __ballot_sync(0xffffffffu, need);
+                    if (need) {
+                        const int k = n1 + __popc(m & below);
+                        Q.idx1[warp][k] = (int)(v - vbase);
+                        Q.pos1[warp][k] = make_float4(pt.x, pt.y, pt.z, w);
+                    }
+                    n1 += __popc(m);
+                    if (n1 >= 32) follow_stage1(fg, vbase, Q, warp, lane, n1, n2);
+                } else {
+                    float d = 0.0f;
+                    if (need) d = fg.sdf8 ? sdf_lookup8(fg.sdf8, fg.sg, pt) : sdf_lookup(fg.sdf, fg.sg, pt);
+                    const bool near = need && d <= fg.margin;
+                    const unsigned m = __ballot_sync(0xffffffffu, near);
+                    if (near) {
+                        const int k = n2 + __popc(m & below);
+                        Q.idx2[warp][k] = (int)(v - vbase);
+                        Q.pos2[warp][k] = make_float4(pt.x, pt.y, pt.z, w);
+                        Q.dist2[warp][k] = d;
+                    }
+                    n2 += __popc(m);
+                    if (n2 >= 32) follow_stage2(fg, vbase, Q, warp, lane, n2);
                 }
-                n1 += __popc(m);
-                if (n1 >= 32) follow_stage1(fg, vbase, Q, warp, lane, n1, n2);
             }
         }
         while (n1 > 0) follow_stage1(fg, vbase, Q, warp, lane, n1, n2);
@@ -1063,18 +1080,23 @@ int follow_max_chunks_per_item(int n) { return (fused_group_strands(n) * n + 255
 
 template <int N>
 static cudaError_t launch_follow_n(const FollowLaunch& fl, cudaStream_t s) {
-    if (fl.queued) k_follow_collide_queued<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
-    else k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+    if (fl.queued == 1)
+        k_follow_collide_queued<N, true><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+    else if (fl.queued == 2)
+        k_follow_collide_queued<N, false><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+    else
+        k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
     return cudaGetLastError();
 }
 
-int follow_blocks_per_sm(int n, bool queued) {
+int follow_blocks_per_sm(int n, int mode) {
     int nb = 0;
     cudaError_t e = cudaErrorInvalidValue;
-#define TFX_FOLLOW_OCC(NN)                                                                                      \
-    case NN:                                                                                                    \
-        e = queued ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide_queued<NN>, 256, 0) \
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<NN>, 256, 0);        \
+#define TFX_FOLLOW_OCC(NN)                                                                                            \
+    case NN:                                                                                                          \
+        e = mode == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide_queued<NN, true>, 256, 0)  \
+            : mode == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide_queued<NN, false>, 256, 0) \
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<NN>, 256, 0);            \
         break;
     switch (n) {
         TFX_FOLLOW_OCC(4)
