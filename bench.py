@@ -580,7 +580,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="head", choices=list(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--autotune", type=int, default=2, help="frames per candidate shape (0: defaults)")
+    ap.add_argument("--autotune", type=int, default=4, help="frames per candidate shape (0: defaults)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--objects", type=int, default=64,
                     help="--config batched: the first N objects of its seeded draw (a small case for profiling)")
