@@ -355,9 +355,15 @@ typedef enum tfx_batch_option {
                                        objects make at least 4 lookups per cell each frame          */
     TFX_BATCH_OVERLAP_SDF = 2,      /* 1: the SDF build runs concurrently with the strand kernels    */
     TFX_BATCH_SDF_BLOCK = 3,        /* threads per block of the SDF construct: 64, 128 or 256         */
-    TFX_BATCH_SPLIT_SWEEPS = 4      /* 1: the local-shape sweeps run as their own launch (a thread per
+    TFX_BATCH_SPLIT_SWEEPS = 4,     /* 1: the local-shape sweeps run as their own launch (a thread per
                                        strand, up to four sweeps pipelined in registers) between two
                                        passes of the strand kernel; 0: inside the strand kernel      */
+    TFX_BATCH_FOLLOW_FORM = 5       /* the follow-hair + collision kernel of every class: 0 one vertex
+                                       at a time per thread; 1 the vertices needing a lookup, then
+                                       those within the margin, queued per warp and processed 32 at
+                                       a time; 2 only the gradient stage queued.  Default per class:
+                                       1 with follow hairs, else 2 at n >= 64, else 0 (get_option
+                                       reports the first class's)                                   */
 } tfx_batch_option;
 /* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
  * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (format

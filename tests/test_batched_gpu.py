@@ -242,3 +242,27 @@ def test_batched_split_sweeps_bit_exact(ctx, n, iters, split):
         assert_same(gpu.hair[0], ora.hair[0], f"n={n} iters={iters} split={split}")
     finally:
         gpu.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1, 2])
+@pytest.mark.parametrize("n,follows", [(16, 0), (16, 2), (64, 0), (64, 1)])
+def test_batched_follow_forms_bit_exact(ctx, form, n, follows):
+    """Every form of the follow-hair + collision kernel (one vertex at a time, both lookup stages on
+    per-warp queues, the gradient stage alone queued) gives the oracle's buffers, with and without
+    follow hairs, on hair lying against the collision mesh."""
+    sc = scene_head(seed=41 + n + follows, num_guides=180, n=n, follows=follows, triangles=2500, sdf_cells=40,
+                    frames=5)
+    gpu = BatchedPipeline(ctx, sc)
+    try:
+        gpu.batch.set_option(gpu.batch.FOLLOW_FORM, form)
+        assert gpu.batch.get_option(gpu.batch.FOLLOW_FORM) == form
+        ora = OraclePipeline(sc)
+        for f in range(5):
+            fin = gpu.step(f)
+            ora.step(fin)
+        assert_same(gpu.hair[0], ora.hair[0], f"form={form} n={n} follows={follows}")
+        with pytest.raises(Exception):
+            gpu.batch.set_option(gpu.batch.FOLLOW_FORM, 3)
+    finally:
+        gpu.close()

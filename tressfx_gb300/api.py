@@ -404,7 +404,7 @@ class Batch:
     def build(self) -> None:
         check(A.lib().tfx_batch_build(self.handle, 0), "tfx_batch_build")
 
-    EXPANDED_GRIDS, OVERLAP_SDF, SDF_BLOCK, SPLIT_SWEEPS = 1, 2, 3, 4
+    EXPANDED_GRIDS, OVERLAP_SDF, SDF_BLOCK, SPLIT_SWEEPS, FOLLOW_FORM = 1, 2, 3, 4, 5
 
     def set_option(self, option: int, value: int) -> None:
         check(A.lib().tfx_batch_set_option(self.handle, option, value), "tfx_batch_set_option")

@@ -890,6 +890,13 @@ extern "C" int tfx_batch_set_option(tfx_batch b, int option, int value) {
             if (value != 0 && value != 1) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: split %d", value);
             for (auto& c : b->classes) c.splitSweeps = value != 0;
             break;
+        case TFX_BATCH_FOLLOW_FORM:
+            if (value < 0 || value > 2) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: follow form %d", value);
+            for (auto& c : b->classes) {
+                c.followMode = value;
+                if (int r = size_class(b, c)) return r;
+            }
+            break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: unknown option %d", option);
     }
     TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
@@ -906,6 +913,7 @@ extern "C" int tfx_batch_get_option(tfx_batch b, int option, int* value) {
         case TFX_BATCH_OVERLAP_SDF: *value = b->overlap ? 1 : 0; break;
         case TFX_BATCH_SDF_BLOCK: *value = b->sdfL.constructThreads; break;
         case TFX_BATCH_SPLIT_SWEEPS: *value = (!b->classes.empty() && b->classes[0].splitSweeps) ? 1 : 0; break;
+        case TFX_BATCH_FOLLOW_FORM: *value = b->classes.empty() ? 0 : b->classes[0].followMode; break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_get_option: unknown option %d", option);
     }
     return TFX_OK;
