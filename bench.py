@@ -64,6 +64,7 @@ NCU_TRAFFIC = {
     # captured on the first 8 objects (5.54 M of the class's 18.69 M vertices, 684.2 MB; the kernel
     # streams each vertex's rows once, so traffic grows with the vertices): scaled to the full launch
     ("batched", "k_fused_strands (n=64)"): 2309.7e6,
+    ("fur", "k_fused_strands (n=16)"): 387.8e6,   # profiles/k_fused_strands_fur_200000x16.md
 }
 
 
