@@ -196,6 +196,11 @@ int tfx_hair_get_buffer(tfx_hair hair, int buffer, void** device_ptr, size_t* by
 /* out[0..3] = total vertices, total strands, vertices per strand, follow hairs per guide
  * (GetNumTotalHairVertices / Strands / VerticesPerStrand / FollowHairsPerGuideHair). */
 int tfx_hair_get_counts(tfx_hair hair, int32_t out[4]);
+/* Health check (report only): counts[0] / counts[1] = vertices of Pos / Prev with a NaN or infinite
+ * component, after the work queued so far (synchronous).  The reference's only guard is the
+ * velocity clamp (TressFXSimulation.hlsl:959-964), which a NaN passes through; the caller resets or
+ * restores the object when a count is non-zero. */
+int tfx_hair_count_nonfinite(tfx_hair hair, int64_t counts[2]);
 
 /* ---------------------------------------------------------------------------------- strand quads */
 /* TressFXStrandParams (TressFXConstantBuffers.h) = cbuffer TressFXStrandParameters
@@ -268,11 +273,15 @@ int tfx_sdf_get_buffer(tfx_sdf sdf, void** device_ptr, size_t* bytes);
 #define TFX_SDF_STATIC_MAX_CELLS 2097152
 /* No counterpart in the reference.  Initialize + Construct + Finalize of `grid` from a DEVICE mesh
  * ({float4 position, float4 normal}[num_vertices], uint32[3*num_triangles]) into the DEVICE float
- * buffer sdf_out[X*Y*Z], the same grid tfx_sdf_update builds, without allocating anything: the
- * FloatFlip3 build words live in one static device array per device (TFX_SDF_STATIC_MAX_CELLS
- * words; larger grids return TFX_ERR_SIZE).  Nothing has to be zeroed first.  The first call on a
- * device looks the array up (make it before any stream capture).  Calls that can overlap on one
- * device (other contexts or streams) race on that array; calls on one context are stream-ordered. */
+ * buffer sdf_out[X*Y*Z], the same grid tfx_sdf_update builds, without allocating anything: for
+ * callers that may not allocate device memory once running (an engine with a fixed GPU memory
+ * budget set at start-up, or a frame being recorded for replay).  The FloatFlip3 build words live
+ * in one static device array per device (TFX_SDF_STATIC_MAX_CELLS words; larger grids return
+ * TFX_ERR_SIZE).  Nothing has to be zeroed first.  The first call on a context looks the array's
+ * address up and keeps it in the context (make that call before any stream capture).  Calls that
+ * can overlap on one device (other contexts or streams) race on that array; calls on one context
+ * are stream-ordered.  Triangle indices must be below num_vertices: they are not checked.  The
+ * caller's current device is left as it was. */
 int tfx_sdf_build_static(tfx_context ctx, const tfx_sdf_grid* grid, const void* mesh_vertices, int num_vertices,
                          const uint32_t* indices, int num_triangles, float* sdf_out);
 
@@ -358,12 +367,16 @@ typedef enum tfx_batch_option {
     TFX_BATCH_SPLIT_SWEEPS = 4,     /* 1: the local-shape sweeps run as their own launch (a thread per
                                        strand, up to four sweeps pipelined in registers) between two
                                        passes of the strand kernel; 0: inside the strand kernel      */
-    TFX_BATCH_FOLLOW_FORM = 5       /* the follow-hair + collision kernel of every class: 0 one vertex
+    TFX_BATCH_FOLLOW_FORM = 5,      /* the follow-hair + collision kernel of every class: 0 one vertex
                                        at a time per thread; 1 the vertices needing a lookup, then
                                        those within the margin, queued per warp and processed 32 at
                                        a time; 2 only the gradient stage queued.  Default per class:
                                        1 with follow hairs, else 2 at n >= 64, else 0 (get_option
                                        reports the first class's)                                   */
+    TFX_BATCH_WAIT_POLLS = 6        /* polls of the strand kernel's bounded wait for a group's bulk
+                                       copies before its block gives up and the frame reports
+                                       TFX_ERR_TIMEOUT (default 2^21; 0 gives up at once, for tests
+                                       of that path).  Not a launch shape: the autotuner leaves it */
 } tfx_batch_option;
 /* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
  * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (format
@@ -392,6 +405,12 @@ int tfx_batch_set_sdf_frame(tfx_batch batch, int index, const tfx_sdf_grid* grid
 int tfx_batch_set_mesh_bones(tfx_batch batch, int index, const float* bone_matrices, int num_bones);
 /* Launches one frame on the context's stream (asynchronous). */
 int tfx_batch_run(tfx_batch batch);
+/* Waits until every frame queued by tfx_batch_run has executed.  Returns TFX_ERR_TIMEOUT, once, if one
+ * of them had a strand block give up its bounded wait (tfx_batch_run itself reports it when it next
+ * reuses that frame's pinned block); that frame's state is then undefined and the caller restores it
+ * (tfx_hair_write) or resets the objects.  No counterpart in the reference (D3D has no device-side
+ * timeout); cudaStreamSynchronize on the context's stream plus the check. */
+int tfx_batch_synchronize(tfx_batch batch);
 /* The launch shapes in use, as text, and the number of kernels one frame launches. */
 int tfx_batch_describe(tfx_batch batch, char* buf, size_t len, int32_t* launches_per_frame);
 /* Runs one frame like tfx_batch_run but with direct launches and CUDA events between its parts;

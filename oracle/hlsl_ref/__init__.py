@@ -20,7 +20,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 REF_DIR = HERE.parent / "_ref"
 LIB = REF_DIR / "libtfx_hlsl_ref.so"
-SHADER_ROOT = Path("/root/reference")
+SHADER_ROOT = Path(os.environ.get("TFX_REFERENCE", "/root/reference"))
 
 _lib = None
 

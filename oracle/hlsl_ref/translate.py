@@ -26,11 +26,12 @@ The output is wrapped in a namespace per shader file and compiled against hlsl_s
 """
 from __future__ import annotations
 
+import os
 import re
 import sys
 from pathlib import Path
 
-REF = Path("/root/reference")
+REF = Path(os.environ.get("TFX_REFERENCE", "/root/reference"))
 SHADERS = {
     "ref_sim": "src/Shaders/TressFXSimulation.hlsl",
     "ref_sdf": "src/Shaders/TressFXSDFCollision.hlsl",

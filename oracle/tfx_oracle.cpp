@@ -30,9 +30,9 @@
 //      the shader targets all lanes read before any lane writes; this restatement therefore
 //      computes every wind displacement from the pre-wind positions (a Jacobi update).
 //
-//  Parity status: see oracle/README.md and the header of oracle/hlsl_ref (the reference's own
-//  shader source compiled as C++), against which this restatement is pinned by
-//  tests/test_oracle_pin.py.
+//  Parity status: pinned bit for bit by tests/test_oracle_pin.py to the reference's own shader
+//  source compiled as C++ (oracle/hlsl_ref), and carried to machines without the reference tree by
+//  the golden fixtures under tests/golden.
 // ============================================================================================
 
 #include <algorithm>

@@ -217,6 +217,8 @@ _PROTOS = {
     "tfx_batch_set_sdf_frame": (C.c_int, [P, C.c_int, C.POINTER(SdfGrid), F32]),
     "tfx_batch_set_mesh_bones": (C.c_int, [P, C.c_int, P, C.c_int]),
     "tfx_batch_run": (C.c_int, [P]),
+    "tfx_batch_synchronize": (C.c_int, [P]),
+    "tfx_hair_count_nonfinite": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "tfx_batch_describe": (C.c_int, [P, C.c_char_p, C.c_size_t, C.POINTER(C.c_int32)]),
     "tfx_batch_profile_frame": (C.c_int, [P, FP, C.c_int, C.POINTER(C.c_int)]),
 }

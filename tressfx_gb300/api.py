@@ -26,6 +26,7 @@ class Context:
         h = C.c_void_p()
         check(A.lib().tfx_context_create(device, C.byref(h)), "tfx_context_create")
         self.handle = h
+        self.device = device
 
     def synchronize(self) -> None:
         check(A.lib().tfx_context_synchronize(self.handle), "tfx_context_synchronize")
@@ -160,6 +161,12 @@ class HairObject(SimConstants):
         if kind == "v1":
             return (self.num_vertices,)
         return (self.num_strands, int(kind[1:]))
+
+    def count_nonfinite(self) -> tuple[int, int]:
+        """Vertices of Pos and of Prev with a NaN or infinite component (report only)."""
+        c = (C.c_int64 * 2)()
+        check(A.lib().tfx_hair_count_nonfinite(self.handle, c), "tfx_hair_count_nonfinite")
+        return int(c[0]), int(c[1])
 
     def read(self, buf: int, out: np.ndarray | None = None) -> np.ndarray:
         if out is None:
@@ -404,7 +411,7 @@ class Batch:
     def build(self) -> None:
         check(A.lib().tfx_batch_build(self.handle, 0), "tfx_batch_build")
 
-    EXPANDED_GRIDS, OVERLAP_SDF, SDF_BLOCK, SPLIT_SWEEPS, FOLLOW_FORM = 1, 2, 3, 4, 5
+    EXPANDED_GRIDS, OVERLAP_SDF, SDF_BLOCK, SPLIT_SWEEPS, FOLLOW_FORM, WAIT_POLLS = 1, 2, 3, 4, 5, 6
 
     def set_option(self, option: int, value: int) -> None:
         check(A.lib().tfx_batch_set_option(self.handle, option, value), "tfx_batch_set_option")
@@ -431,6 +438,10 @@ class Batch:
 
     def run(self) -> None:
         check(A.lib().tfx_batch_run(self.handle), "tfx_batch_run")
+
+    def synchronize(self) -> None:
+        """Waits for the queued frames; raises TfxError(TFX_ERR_TIMEOUT) once if one of them timed out."""
+        check(A.lib().tfx_batch_synchronize(self.handle), "tfx_batch_synchronize")
 
     READBACK_XYZW, READBACK_XYZ = 0, 1
 

@@ -54,6 +54,9 @@ struct BatchSdf {
     int numTriangles;
 };
 
+// Polls of k_fused_strands' bounded wait for a group's bulk copies before the block gives up.
+constexpr int kFusedWaitPollsDefault = 1 << 21;
+
 struct FusedLaunch {
     int n, vpl, warpsPerBlock, blocks;
     const BatchObject* objs;
@@ -61,6 +64,7 @@ struct FusedLaunch {
     int numItems;
     int* err;        // set to 1 when a block gives up waiting for its bulk copies
     int mode;        // 0 the whole frame, 1 up to the local-shape sweeps, 2 after them
+    int waitPolls;   // limit of the first wait (kFusedWaitPollsDefault; 0 in tests of the timeout path)
 };
 
 struct FollowLaunch {

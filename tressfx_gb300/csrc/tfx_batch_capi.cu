@@ -83,6 +83,7 @@ struct tfx_batch_t {
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
     int* devErr = nullptr;      // fused kernel: a block gave up waiting for its bulk copies
     int* pinnedErr = nullptr;   // its copy at the end of each frame, one word per slot
+    int waitPolls = kFusedWaitPollsDefault;   // TFX_BATCH_WAIT_POLLS
 
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int launchesPerFrame = 0;
@@ -101,6 +102,19 @@ struct tfx_batch_t {
 };
 
 static int batch_fail_built(const char* who) { return fail(TFX_ERR_INVALID_ARGUMENT, "%s: the batch is already built", who); }
+
+// A frame's fused strand kernel gave up waiting for its bulk copies: waits for the frames queued so
+// far, clears the device flag and both frames' copies of it (so the report is made once), and
+// returns TFX_ERR_TIMEOUT.  The state of the failed frame is undefined; the caller restores it
+// (tfx_hair_write) or resets the objects.
+static int report_timeout(tfx_batch b) {
+    cudaSetDevice(b->ctx->device);
+    cudaError_t e = cudaStreamSynchronize(b->ctx->stream);
+    if (e == cudaSuccess) e = cudaMemset(b->devErr, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: clearing the error flag");
+    b->pinnedErr[0] = b->pinnedErr[1] = 0;
+    return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+}
 
 extern "C" int tfx_batch_create(tfx_context ctx, tfx_batch* out) {
     if (!out || !ctx) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_create: null argument");
@@ -250,7 +264,7 @@ static int launch_sdf_part(tfx_batch b, cudaStream_t s) {
 }
 
 static int launch_strands(tfx_batch b, BatchClass& c, cudaStream_t s) {
-    FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems, b->devErr, 0};
+    FusedLaunch fl{c.n, c.vpl, c.warps, c.blocks, b->objTable, c.items, c.numItems, b->devErr, 0, b->waitPolls};
     cudaError_t e;
     if (!c.splitSweeps) {
         e = launch_fused_strands(fl, s);
@@ -301,7 +315,7 @@ static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* 
         cudaMemcpy(&flag, b->devErr, sizeof(int), cudaMemcpyDeviceToHost);
         if (flag) {
             for (auto e : ev) cudaEventDestroy(e);
-            return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+            return report_timeout(b);
         }
         partMs->clear();
         for (size_t i = 1; i < ev.size(); ++i) {
@@ -434,7 +448,7 @@ static int time_graph_frames(tfx_batch b, int frames, float* ms) {
     if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: autotune frames");
     int flag = 0;
     TFX_CUDA(cudaMemcpy(&flag, b->devErr, sizeof(int), cudaMemcpyDeviceToHost), "tfx_batch: error flag");
-    if (flag) return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+    if (flag) return report_timeout(b);
     *ms = best;
     return TFX_OK;
 }
@@ -766,7 +780,10 @@ static int claim_block(tfx_batch b, int* slotOut) {
     b->slot ^= 1;
     if (b->used[s]) {
         TFX_CUDA(cudaEventSynchronize(b->done[s]), "cudaEventSynchronize");
-        if (b->pinnedErr[s]) return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
+        if (b->pinnedErr[s]) {
+            b->slot = s;   // the block stays unclaimed: the next call takes it
+            return report_timeout(b);
+        }
     }
     std::memcpy(b->pinned[s], b->staging.data(), b->blockBytes);
     *slotOut = s;
@@ -781,6 +798,15 @@ extern "C" int tfx_batch_run(tfx_batch b) {
     TFX_CUDA(cudaGraphLaunch(b->graph[s], b->ctx->stream), "cudaGraphLaunch");
     TFX_CUDA(cudaEventRecord(b->done[s], b->ctx->stream), "cudaEventRecord");
     b->used[s] = true;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_synchronize(tfx_batch b) {
+    if (!b || !b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_synchronize: batch not built");
+    TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
+    TFX_CUDA(cudaStreamSynchronize(b->ctx->stream), "cudaStreamSynchronize");
+    for (int s = 0; s < 2; ++s)
+        if (b->used[s] && b->pinnedErr[s]) return report_timeout(b);
     return TFX_OK;
 }
 
@@ -897,6 +923,10 @@ extern "C" int tfx_batch_set_option(tfx_batch b, int option, int value) {
                 if (int r = size_class(b, c)) return r;
             }
             break;
+        case TFX_BATCH_WAIT_POLLS:
+            if (value < 0) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: wait polls %d", value);
+            b->waitPolls = value;
+            break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: unknown option %d", option);
     }
     TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
@@ -914,6 +944,7 @@ extern "C" int tfx_batch_get_option(tfx_batch b, int option, int* value) {
         case TFX_BATCH_SDF_BLOCK: *value = b->sdfL.constructThreads; break;
         case TFX_BATCH_SPLIT_SWEEPS: *value = (!b->classes.empty() && b->classes[0].splitSweeps) ? 1 : 0; break;
         case TFX_BATCH_FOLLOW_FORM: *value = b->classes.empty() ? 0 : b->classes[0].followMode; break;
+        case TFX_BATCH_WAIT_POLLS: *value = b->waitPolls; break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_get_option: unknown option %d", option);
     }
     return TFX_OK;

@@ -170,7 +170,6 @@ __host__ __device__ constexpr int fused_group_strands(int n) { return n >= 64 ? 
 __host__ __device__ constexpr int fused_smem_for(int n) {
     return 2 * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * 7 * 16 + 16;
 }
-constexpr int kFusedWaitPolls = 1 << 21;
 // k_fused_strands modes: the whole frame of the group, or its part before the local-shape sweeps
 // (integration, strand-level data, VSP; the state goes to global memory for k_local_sweep), or its
 // part after them (wind, length constraints, tangents, velocity clamp)
@@ -285,7 +284,7 @@ __device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const f
 template <int N, int VPL>
 __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused_strands(const BatchObject* __restrict__ objs,
                                                                         const WorkItem* __restrict__ items, int numItems,
-                                                                        int* err, int mode) {
+                                                                        int* err, int mode, int waitPolls) {
     constexpr int GS = fused_group_strands(N);
     constexpr int RS = N + 1;       // tile row stride, float4
     constexpr int L = N / VPL;      // lanes per strand in the per-strand passes
@@ -340,10 +339,14 @@ __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused
                 bq4 = make_float4(bq.x, bq.y, bq.z, bq.w);
             }
         }
-        const bool arrived = mbar_wait_bounded(bar, parity, kFusedWaitPolls);
+        // waitPolls is kFusedWaitPollsDefault except in tests of this path (0: give up at once).  On
+        // giving up, the block waits again with the full limit for its copies in flight to land before
+        // it returns; if that wait gives up too, the block returns regardless (the frame is reported
+        // as failed, and a bounded wait is preferred over one that could hang the device).
+        const bool arrived = mbar_wait_bounded(bar, parity, waitPolls);
         if (__syncthreads_or(!arrived)) {
             if (tid == 0) atomicOr(err, 1);
-            mbar_wait_bounded(bar, parity, kFusedWaitPolls);   // let copies still in flight land
+            mbar_wait_bounded(bar, parity, kFusedWaitPollsDefault);
             return;
         }
 
@@ -981,7 +984,7 @@ __global__ void __launch_bounds__(256) k_snapshot_positions(const BatchObject* _
 cudaError_t launch_snapshot_positions(const BatchObject* objs, const long long* first, int nobj, long long total,
                                       float* out, int xyzOnly, cudaStream_t s) {
     if (total <= 0) return cudaSuccess;
-    const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, 152LL * 16);
+    const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, (long long)sm_count() * 16);
     k_snapshot_positions<<<blocks, 256, 0, s>>>(objs, first, nobj, total, out, xyzOnly);
     return cudaGetLastError();
 }
@@ -992,7 +995,7 @@ template <int N, int VPL>
 static cudaError_t launch_fused_nv(const FusedLaunch& fl, cudaStream_t s) {
     // the dynamic shared-memory attribute is set by fused_blocks_per_sm before the first launch
     k_fused_strands<N, VPL><<<fl.blocks, fl.warpsPerBlock * 32, fused_smem_for(N), s>>>(fl.objs, fl.items, fl.numItems,
-                                                                                        fl.err, fl.mode);
+                                                                                        fl.err, fl.mode, fl.waitPolls);
     return cudaGetLastError();
 }
 
@@ -1131,17 +1134,17 @@ cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int tot
 cudaError_t launch_batch_sdf(const SdfBatchLaunch& L, cudaStream_t s) {
     if (L.nsdf <= 0) return cudaSuccess;
     const long long q = L.totalQuads;
-    const unsigned gq = (unsigned)std::min<long long>((q + 255) / 256, 152LL * 32);
+    const unsigned gq = (unsigned)std::min<long long>((q + 255) / 256, (long long)sm_count() * 32);
     k_batch_sdf_init<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
     if (L.totalTris > 0) {
         const int warpsPerBlock = L.constructThreads / 32;
         const long long blocks = (L.totalTris + warpsPerBlock - 1) / warpsPerBlock;
-        k_batch_sdf_construct<<<(unsigned)std::min<long long>(blocks, 152LL * 64), L.constructThreads, 0, s>>>(
+        k_batch_sdf_construct<<<(unsigned)std::min<long long>(blocks, (long long)sm_count() * 64), L.constructThreads, 0, s>>>(
             L.sdfs, L.nsdf, L.totalTris);
     }
     k_batch_sdf_finalize<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
     if (L.expand) {
-        const unsigned ge = (unsigned)std::min<long long>((4 * q + 255) / 256, 152LL * 32);
+        const unsigned ge = (unsigned)std::min<long long>((4 * q + 255) / 256, (long long)sm_count() * 32);
         k_batch_sdf_expand<<<ge, 256, 0, s>>>(L.sdfs, L.nsdf, q);
     }
     return cudaGetLastError();

@@ -251,6 +251,8 @@ extern "C" int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* d, const fl
     for (int b = 1; b <= 9; ++b) { offs[b] = total; total += align256(sizes[b]); }
     offs[10] = total;
     total += align256(sizeof(DevSimConsts));
+    const size_t healthOff = total;   // tfx_hair_count_nonfinite's two counters
+    total += align256(2 * sizeof(unsigned long long));
 
     cudaError_t e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) { h->arena = nullptr; hair_free(h); return cuda_fail(e, "tfx_hair_create: cudaMalloc"); }
@@ -258,6 +260,7 @@ extern "C" int tfx_hair_create(tfx_context ctx, const tfx_hair_desc* d, const fl
     char* base = (char*)h->arena;
     for (int b = 1; b <= 9; ++b) h->bufs[b] = {base + offs[b], sizes[b]};
     h->consts = (DevSimConsts*)(base + offs[10]);
+    h->health = (unsigned long long*)(base + healthOff);
     for (int i = 0; i < 2; ++i) {
         e = cudaMallocHost((void**)&h->staging[i], sizeof(DevSimConsts));
         if (e != cudaSuccess) { h->staging[i] = nullptr; hair_free(h); return cuda_fail(e, "tfx_hair_create: cudaMallocHost"); }

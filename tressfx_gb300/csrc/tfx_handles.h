@@ -20,6 +20,7 @@ struct tfx_context_t {
     std::atomic<int> refs{1};
     std::vector<std::string> stampNames;
     std::vector<cudaEvent_t> stampEvents;
+    uint32_t* sdfStaticWords = nullptr;   // device address of tfx_sdf_build_static's array, once looked up
 };
 
 struct tfx_hair_t {
@@ -36,6 +37,7 @@ struct tfx_hair_t {
     bool stagingUsed[2] = {false, false};
     int stagingNext = 0;
     struct Buf { void* ptr; size_t bytes; } bufs[10]{};
+    unsigned long long* health = nullptr;          // device: non-finite counts of Pos and Prev
 };
 
 struct tfx_sdf_t {

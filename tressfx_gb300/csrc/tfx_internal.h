@@ -43,6 +43,10 @@ struct SdfGrid {
     int nx, ny, nz, reserved;
 };
 
+// Streaming multiprocessors of the current device, looked up once per device ordinal.  Grid-stride
+// launches size their grids as a multiple of it.
+int sm_count();
+
 // Launchers (tfx_sim_kernels.cu / tfx_sdf_kernels.cu). Return cudaGetLastError() of the launch.
 cudaError_t launch_integrate(const HairView& h, cudaStream_t s);
 cudaError_t launch_strand_level(const HairView& h, cudaStream_t s);

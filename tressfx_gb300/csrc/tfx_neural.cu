@@ -676,7 +676,7 @@ cudaError_t launch_query(const __nv_bfloat16* wbf, const float* bias, const Fram
     cudaError_t e = cudaFuncSetAttribute(k_nsdf_query<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
     const int tiles = (count + 31) / 32;
-    const int blocks = std::min((tiles + QUERY_WARPS - 1) / QUERY_WARPS, 152 * 8);
+    const int blocks = std::min((tiles + QUERY_WARPS - 1) / QUERY_WARPS, sm_count() * 8);
     k_nsdf_query<false><<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(wbf, bias, fr, points, nullptr, count, pose, out);
     return cudaGetLastError();
 }
@@ -687,7 +687,7 @@ cudaError_t launch_query_samples(const __nv_bfloat16* wbf, const float* bias, co
     cudaError_t e = cudaFuncSetAttribute(k_nsdf_query<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
     const int tiles = (count + 31) / 32;
-    const int blocks = std::min((tiles + QUERY_WARPS - 1) / QUERY_WARPS, 152 * 8);
+    const int blocks = std::min((tiles + QUERY_WARPS - 1) / QUERY_WARPS, sm_count() * 8);
     k_nsdf_query<true><<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(wbf, bias, fr, nullptr, samples, count, Pose{0, 0, 0},
                                                                     out);
     return cudaGetLastError();
@@ -700,7 +700,7 @@ cudaError_t launch_train_step(const __nv_bfloat16* wbf, const float* bias, const
     cudaError_t e = cudaFuncSetAttribute(k_nsdf_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRAIN_SMEM);
     if (e != cudaSuccess) return e;
     const int tiles = batch / 16;
-    const int blocks = std::min((tiles + TRAIN_WARPS - 1) / TRAIN_WARPS, 152 * 2);
+    const int blocks = std::min((tiles + TRAIN_WARPS - 1) / TRAIN_WARPS, sm_count() * 2);
     k_nsdf_train<<<blocks, TRAIN_WARPS * 32, TRAIN_SMEM, s>>>(wbf, bias, fr, pool, poolSize, batch, seed,
                                                              reinterpret_cast<uint32_t*>(acts), lossSum);
     e = cudaMemsetAsync(grads, 0, sizeof(float) * NPARAM, s);
@@ -855,13 +855,13 @@ cudaError_t launch_collide(const CollideArgs& a, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nsdf_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
     const long long tiles = (a.vtot + 31) / 32;
-    const int blocks = (int)std::min<long long>((tiles + QUERY_WARPS - 1) / QUERY_WARPS, 152 * 8);
+    const int blocks = (int)std::min<long long>((tiles + QUERY_WARPS - 1) / QUERY_WARPS, sm_count() * 8);
     k_nsdf_classify<<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(a);
-    const unsigned gc = (unsigned)std::min<long long>((cells + 255) / 256, 152LL * 16);
+    const unsigned gc = (unsigned)std::min<long long>((cells + 255) / 256, (long long)sm_count() * 16);
     k_gated_init<<<gc, 256, 0, s>>>(a.words, cells, a.bandCount);
-    if (a.ntri > 0) k_gated_construct<<<(unsigned)std::min(( a.ntri + 7) / 8, 152 * 32), 256, 0, s>>>(a);
+    if (a.ntri > 0) k_gated_construct<<<(unsigned)std::min(( a.ntri + 7) / 8, sm_count() * 32), 256, 0, s>>>(a);
     k_gated_finalize<<<gc, 256, 0, s>>>(a.words, cells, a.bandCount);
-    k_band_collide<<<152 * 4, 256, 0, s>>>(a);
+    k_band_collide<<<sm_count() * 4, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 

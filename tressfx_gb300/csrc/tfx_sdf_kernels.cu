@@ -5,6 +5,8 @@
 // over the encoding = min |d|, ties to the positive value) and plain floats after Finalize.
 // atomicMin is order independent, and the distance arithmetic below is the reference's in the
 // same order with no FMA contraction, so the finished grid matches the oracle bit for bit.
+#include <atomic>
+
 #include "tfx_sdf_math.cuh"
 
 namespace tfx {
@@ -131,6 +133,19 @@ __global__ void __launch_bounds__(256) k_mesh_skin(float4* __restrict__ out, con
 }
 
 // --------------------------------------------------------------------------------------------
+int sm_count() {
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 1;
+        cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
 static inline unsigned grid_for(long long work, int threads, unsigned cap) {
     long long b = (work + threads - 1) / threads;
     if (b < 1) b = 1;
@@ -139,21 +154,21 @@ static inline unsigned grid_for(long long work, int threads, unsigned cap) {
 
 cudaError_t launch_sdf_initialize(uint32_t* sdf, int64_t cells, cudaStream_t s) {
     if (cells <= 0) return cudaSuccess;
-    k_sdf_initialize<<<grid_for((cells + 3) / 4, 256, 152 * 16), 256, 0, s>>>(sdf, cells);
+    k_sdf_initialize<<<grid_for((cells + 3) / 4, 256, sm_count() * 16), 256, 0, s>>>(sdf, cells);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sdf_construct(uint32_t* sdf, const SdfGrid& g, const float4* mesh, const uint32_t* idx, int ntri,
                                  cudaStream_t s) {
     if (ntri <= 0) return cudaSuccess;
-    k_sdf_construct<<<(unsigned)std::min<long long>(((long long)ntri + 3) / 4, 152LL * 64), 128, 0, s>>>(sdf, g, mesh,
+    k_sdf_construct<<<(unsigned)std::min<long long>(((long long)ntri + 3) / 4, (long long)sm_count() * 64), 128, 0, s>>>(sdf, g, mesh,
                                                                                                  idx, ntri);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sdf_finalize(uint32_t* sdf, int64_t cells, cudaStream_t s) {
     if (cells <= 0) return cudaSuccess;
-    k_sdf_finalize<<<grid_for((cells + 3) / 4, 256, 152 * 16), 256, 0, s>>>(sdf, cells);
+    k_sdf_finalize<<<grid_for((cells + 3) / 4, 256, sm_count() * 16), 256, 0, s>>>(sdf, cells);
     return cudaGetLastError();
 }
 
