@@ -29,6 +29,32 @@ class HairStruct(C.Structure):
                 ("follow_offset", C.c_void_p), ("skin", C.c_void_p)]
 
 
+class Settings(C.Structure):
+    """TressFXSimulationSettings (TressFXSettings.h:59-87), field for field."""
+    _fields_ = [("vsp_coeff", C.c_float), ("vsp_accel_threshold", C.c_float),
+                ("local_constraint_stiffness", C.c_float), ("local_constraints_iterations", C.c_int32),
+                ("global_constraint_stiffness", C.c_float), ("global_constraints_range", C.c_float),
+                ("length_constraints_iterations", C.c_int32), ("damping", C.c_float),
+                ("gravity_magnitude", C.c_float), ("tip_separation", C.c_float), ("wind_magnitude", C.c_float),
+                ("wind_direction", C.c_float * 3), ("wind_angle_radians", C.c_float),
+                ("clamp_position_delta", C.c_float)]
+
+
+class SimParams(C.Structure):
+    """TressFXSimulationParams (TressFXConstantBuffers.h:41-85): the 160-byte header, then 512 bone
+    matrices (16 floats each, row-major)."""
+    _fields_ = [("header", C.c_uint8 * 160), ("bones", C.c_float * (512 * 16))]
+
+    def header_bytes(self) -> bytes:
+        return bytes(self.header)
+
+    def bones_view(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.bones).reshape(512, 16)
+
+    def set_reset(self, value: float) -> None:
+        C.c_float.from_buffer(self.header, 144).value = value
+
+
 class SdfParams(C.Structure):
     _fields_ = [("origin", C.c_float * 4), ("cell_size", C.c_float), ("nx", C.c_int32), ("ny", C.c_int32),
                 ("nz", C.c_int32)]
@@ -46,6 +72,9 @@ def lib() -> C.CDLL:
             getattr(l, f"tfxo_sdf_build_{suf}").argtypes = [vp, vp, vp, vp, i64, i32]
             getattr(l, f"tfxo_sdf_collide_{suf}").argtypes = [vp, vp, C.c_float, C.POINTER(HairStruct), i32]
         l.tfxo_sdf_construct_f32.argtypes = [vp, vp, vp, vp, i64, i32]
+        l.tfxo_settings_default.argtypes = [C.POINTER(Settings)]
+        l.tfxo_fill_sim_params.argtypes = [C.POINTER(Settings), C.c_float, i32, i32, i32, C.POINTER(SimParams)]
+        l.tfxo_fill_sim_params.restype = C.c_int
         l.tfxo_signed_distance_triangle_f32.argtypes = [vp, vp, vp, vp]
         l.tfxo_signed_distance_triangle_f32.restype = C.c_float
         l.tfxo_float_flip3.argtypes = [C.c_float]
@@ -199,3 +228,21 @@ def float_flip3(f: float) -> int:
 
 def ifloat_flip3(u: int) -> int:
     return int(lib().tfxo_ifloat_flip3(u))
+
+
+def settings(**overrides) -> Settings:
+    """The reference's default settings, then the given fields (names as in the Settings struct)."""
+    st = Settings()
+    lib().tfxo_settings_default(C.byref(st))
+    for k, v in overrides.items():
+        if k == "wind_direction":
+            for i in range(3):
+                st.wind_direction[i] = float(v[i])
+        else:
+            setattr(st, k, v)
+    return st
+
+
+def fill_sim_params(params: SimParams, st: Settings, dt: float, n: int, F: int, frame: int) -> int:
+    """UpdateSimulationParameters on `params`; returns the CPU local-shape iteration count."""
+    return int(lib().tfxo_fill_sim_params(C.byref(st), float(dt), int(n), int(F), int(frame), C.byref(params)))

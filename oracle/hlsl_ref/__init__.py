@@ -70,12 +70,12 @@ class RefPipeline:
 
     def __init__(self, scene):
         import oracle
-        from tressfx_gb300.api import SimConstants
-        from tressfx_gb300.synthetic import margin_world
+        from oracle.consts_ref import ReferenceConstants
+        from oracle.scene_driver import margin_world
         self._margin_world = margin_world
         self.scene = scene
         self.hair = [oracle.OracleHair(o.asset) for o in scene.objects]
-        self.consts = [SimConstants(o.asset.verts_per_strand, o.asset.follow_per_guide) for o in scene.objects]
+        self.consts = [ReferenceConstants(o.asset.verts_per_strand, o.asset.follow_per_guide) for o in scene.objects]
         self.sdf_words = [None] * len(scene.objects)
         self.skinned = [None] * len(scene.objects)
         self.frame = 0
@@ -121,7 +121,7 @@ class RefPipeline:
     def step(self, fin, per_stage=None) -> None:
         sc = self.scene
         for i, c in enumerate(self.consts):
-            c.update_simulation_parameters(fin.settings[i], sc.dt)
+            c.update_simulation_parameters(fin.settings_overrides[i], sc.dt)
             c.update_bone_matrices(fin.hair_bones[i])
         for i, o in enumerate(sc.objects):
             if o.mesh is not None:

@@ -2,8 +2,9 @@
 
 Mirrors tressfx_gb300.headless.PlainPipeline step for step -- skin meshes, rebuild SDFs,
 simulate (stage-major over objects), collide -- with every kernel replaced by the oracle's
-restatement.  Constant blocks come from the same host code (tressfx_gb300.api.SimConstants), so
-the GPU and the oracle consume identical inputs.
+restatement.  The constant blocks are the oracle's own (tfxo_fill_sim_params, pinned bit for bit to
+the reference's TressFXHairObject code by tests/test_consts_pin.py), so this driver never loads the
+CUDA library: only the scene description and the per-frame inputs (numpy) are shared with it.
 """
 from __future__ import annotations
 
@@ -12,19 +13,51 @@ import time
 import numpy as np
 
 from . import OracleHair, STAGE_FOLLOW, STAGE_INTEGRATE, STAGE_LENGTH_WIND, STAGE_LOCAL_SHAPE, STAGE_STRAND_LEVEL, \
-    STAGE_VSP, mesh_skin, sdf_build, sdf_collide
+    STAGE_VSP, SimParams, fill_sim_params, mesh_skin, sdf_build, sdf_collide, settings
+
+
+class OracleConstants:
+    """The host half of TressFXHairObject (TressFXHairObject.h:104, 129; TressFXHairObject.cpp:157,
+    366-437): two constant blocks used alternately by frame parity, the frame counter, the reset flag
+    and the CPU local-shape iteration count."""
+
+    def __init__(self, n: int, F: int):
+        self.n, self.F = n, F
+        self.blocks = [SimParams(), SimParams()]
+        self.frame = 0
+        self.cpu_local_iterations = 0
+        self.blocks[0].set_reset(1.0)   # the constructor's ResetPositions
+
+    def update_simulation_parameters(self, overrides: dict, dt: float) -> None:
+        self.cpu_local_iterations = fill_sim_params(self.blocks[self.frame % 2], settings(**overrides), dt, self.n,
+                                                    self.F, self.frame)
+
+    def update_bone_matrices(self, mats: np.ndarray) -> None:
+        mats = np.ascontiguousarray(mats, dtype=np.float32).reshape(-1, 16)
+        k = min(len(mats), 512)
+        self.blocks[self.frame % 2].bones_view()[:k] = mats[:k]
+
+    def increase_simulation_frame(self) -> None:
+        self.blocks[self.frame % 2].set_reset(0.0)
+        self.frame += 1
+
+    def current_params(self) -> SimParams:
+        return self.blocks[self.frame % 2]
+
+
+def margin_world(obj, grid) -> float:
+    """collisionMargin * cellSize in float (TressFXSDFCollision.cpp:194)."""
+    return float(np.float32(obj.collision_margin_cells) * np.float32(grid.cell_size))
 
 
 class OraclePipeline:
     def __init__(self, scene, dtype=np.float32, threads: int = 0):
-        from tressfx_gb300.api import SimConstants
-        from tressfx_gb300.synthetic import margin_world
         self._margin_world = margin_world
         self.scene = scene
         self.dtype = np.dtype(dtype)
         self.threads = threads
         self.hair = [OracleHair(o.asset, dtype) for o in scene.objects]
-        self.consts = [SimConstants(o.asset.verts_per_strand, o.asset.follow_per_guide) for o in scene.objects]
+        self.consts = [OracleConstants(o.asset.verts_per_strand, o.asset.follow_per_guide) for o in scene.objects]
         self.sdf_words = [None] * len(scene.objects)
         self.frame = 0
         self.stage_seconds: dict[str, float] = {}
@@ -37,7 +70,7 @@ class OraclePipeline:
     def step(self, fin) -> None:
         sc = self.scene
         for i, (h, c) in enumerate(zip(self.hair, self.consts)):
-            c.update_simulation_parameters(fin.settings[i], sc.dt)
+            c.update_simulation_parameters(fin.settings_overrides[i], sc.dt)
             c.update_bone_matrices(fin.hair_bones[i])
         t = time.perf_counter()
         for i, o in enumerate(sc.objects):

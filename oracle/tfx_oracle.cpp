@@ -954,3 +954,136 @@ extern "C" int tfxo_marching_cubes_f32(const float* sdf, const SdfParamsF* g, fl
     *counter = (int32_t)count;
     return 0;
 }
+
+// ============================================================================================
+// Host-side constants: TressFXSimulationSettings -> TressFXSimulationParams header.
+// Restates TressFXSettings.h:38-56 (defaults), TressFXHairObject.cpp:380-437
+// (UpdateSimulationParameters), :172-235 (SetWindCorner, SetWind) and the pieces of src/Math the
+// wind uses (Vector3 Cross / Length / Normalize, Vector3D.h:70-75 and Vector3D.cpp:48-62;
+// Quaternion SetRotation / operator* , Quaternion.cpp:79-89, 262-284), in float, in the
+// reference's operation order.  The reference is a Windows build whose unqualified sin / pow / asin
+// on floats are the float functions; they are called as sinf / powf / asinf here.
+// ============================================================================================
+struct SettingsF {   // TressFXSimulationSettings, declaration order (TressFXSettings.h:59-87)
+    float vspCoeff, vspAccelThreshold, localStiffness;
+    int32_t localIterations;
+    float globalStiffness, globalRange;
+    int32_t lengthIterations;
+    float damping, gravity, tipSeparation, windMagnitude, windDirection[3], windAngle, clampPositionDelta;
+};
+static_assert(sizeof(SettingsF) == 64, "layout");
+
+namespace host {
+
+struct Vec { float x, y, z; };
+struct Rot { float x, y, z, w; };   // quaternion, identity = (0, 0, 0, 1)
+
+static Vec cross(Vec a, Vec b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+static float length(Vec a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+static void normalize_in_place(Vec& a) {   // leaves a zero vector unchanged
+    const float d = sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
+    if (d == 0) return;
+    a.x = a.x / d; a.y = a.y / d; a.z = a.z / d;
+}
+static Rot axis_angle(Vec axis, float angle) {
+    const float h = 0.5f * angle;
+    const float s = sinf(h);
+    return {s * axis.x, s * axis.y, s * axis.z, cosf(h)};
+}
+static Rot compose(Rot a, Rot b) {   // a * b
+    Rot q;
+    q.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+    q.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+    q.y = a.w * b.y + a.y * b.w + a.z * b.x - a.x * b.z;
+    q.z = a.w * b.z + a.z * b.w + a.x * b.y - a.y * b.x;
+    return q;
+}
+static Vec rotate(Rot q, Vec v) {   // v + 2w (q x v) + 2 q x (q x v)
+    const Vec qv{q.x, q.y, q.z};
+    Vec uv = cross(qv, v);
+    Vec uuv = cross(qv, uv);
+    const float s = 2.0f * q.w;
+    uv = {uv.x * s, uv.y * s, uv.z * s};
+    uuv = {uuv.x * 2.0f, uuv.y * 2.0f, uuv.z * 2.0f};
+    const Vec a{v.x + uv.x, v.y + uv.y, v.z + uv.z};
+    return {a.x + uuv.x, a.y + uuv.y, a.z + uuv.z};
+}
+
+// one edge of the wind pyramid (SetWindCorner)
+static void wind_corner(Rot toWind, Vec axis, float coneAngle, float wM, float out[4]) {
+    const Vec d = rotate(compose(toWind, axis_angle(axis, coneAngle)), Vec{1.0f, 0.0f, 0.0f});
+    out[0] = d.x * wM;
+    out[1] = d.y * wM;
+    out[2] = d.z * wM;
+    out[3] = 0.0f;
+}
+
+static void set_wind(SimParamsF* p, const float dir[3], float magnitude, int frame) {
+    const float wM = magnitude * (powf(sinf(frame * 0.01f), 2.0f) + 0.5f);
+    Vec w{dir[0], dir[1], dir[2]};
+    normalize_in_place(w);
+    Vec axis = cross(Vec{1.0f, 0.0f, 0.0f}, w);
+    Rot toWind{0.0f, 0.0f, 0.0f, 1.0f};
+    const float angle = asinf(length(axis));
+    if (angle > 0.001) {   // a double comparison, as in the reference
+        normalize_in_place(axis);
+        toWind = axis_angle(axis, angle);
+    }
+    const float cone = 40.f * 3.14159265359f / 180;   // DEG_TO_RAD2(40.f)
+    wind_corner(toWind, Vec{0, 1.0f, 0}, cone, wM, p->wind);
+    wind_corner(toWind, Vec{0, -1.0f, 0}, cone, wM, p->wind1);
+    wind_corner(toWind, Vec{0, 0, 1.0f}, cone, wM, p->wind2);
+    wind_corner(toWind, Vec{0, 0, -1.0f}, cone, wM, p->wind3);
+}
+
+}  // namespace host
+
+extern "C" void tfxo_settings_default(SettingsF* s) {
+    s->vspCoeff = 0.8f;
+    s->vspAccelThreshold = 1.4f;
+    s->localStiffness = 0.9f;
+    s->localIterations = 2;
+    s->globalStiffness = 0.0f;
+    s->globalRange = 0.0f;
+    s->lengthIterations = 2;
+    s->damping = 0.08f;
+    s->gravity = 0.0f;
+    s->tipSeparation = 0.0f;
+    s->windMagnitude = 0.0f;
+    s->windDirection[0] = 1.0f;
+    s->windDirection[1] = 0.0f;
+    s->windDirection[2] = 0.0f;
+    s->windAngle = 3.1415926f / 180.0f * 40.0f;
+    s->clampPositionDelta = 20.f;
+}
+
+// UpdateSimulationParameters on the constant block of the current frame; the reset flag is set for
+// frames 0 and 1 and otherwise left as the block holds it.  Returns m_CPULocalShapeIterations.
+extern "C" int tfxo_fill_sim_params(const SettingsF* s, float timeStep, int n, int F, int frame, SimParamsF* p) {
+    p->vsp[0] = s->vspCoeff;
+    p->vsp[1] = s->vspAccelThreshold;
+    p->shape[0] = s->damping;
+    p->shape[1] = s->localStiffness;
+    p->shape[2] = s->globalStiffness;
+    p->shape[3] = s->globalRange;
+    p->gravTimeTip[0] = s->gravity;
+    p->gravTimeTip[1] = timeStep;
+    p->simInts[2] = 0;                 // SetCollision(false)
+    p->counts[0] = 64 / n;             // TRESSFX_SIM_THREAD_GROUP_SIZE / n
+    p->counts[2] = n;
+    p->counts[1] = F;
+    p->gravTimeTip[2] = s->tipSeparation;
+    p->clampPositionDelta = 20.0f;
+    int cpuIterations;
+    if (n >= 64) {                     // TRESSFX_MIN_VERTS_PER_STRAND_FOR_GPU_ITERATION
+        p->simInts[1] = s->localIterations;
+        cpuIterations = 1;
+    } else {
+        p->simInts[1] = 1;
+        cpuIterations = s->localIterations;
+    }
+    p->simInts[0] = s->lengthIterations;
+    host::set_wind(p, s->windDirection, s->windMagnitude, frame);
+    if (frame < 2) p->resetPositions = 1.0f;
+    return cpuIterations;
+}

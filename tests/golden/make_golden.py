@@ -3,7 +3,8 @@
 Run where the reference checkout is mounted:  python tests/golden/make_golden.py
 Each fixture stores the inputs of a short run and the SHA-256 digest of the simulation state after
 each recorded kernel, as computed by oracle/hlsl_ref (the reference's HLSL compiled as C++,
-dispatched with the reference's own group counts).  tests/golden_replay.py replays them on the
+dispatched with the reference's own group counts).  The constant block of every frame comes from
+oracle/consts_ref (the reference's own UpdateSimulationParameters / SetWind, compiled here).  tests/golden_replay.py replays them on the
 oracle and on the CUDA library.
 """
 from __future__ import annotations
@@ -83,7 +84,8 @@ def cases():
 
 
 def make(name, scene, frames, stage_frames) -> dict:
-    from tressfx_gb300.api import SimConstants
+    import oracle
+    import oracle.consts_ref as R
     from tressfx_gb300.headless import FrameInputs
     from tressfx_gb300.synthetic import margin_world
     from golden_replay import Asset  # noqa: F401
@@ -107,17 +109,21 @@ def make(name, scene, frames, stage_frames) -> dict:
     asset.follow_root_offsets, asset.bone_skinning = a.follow_root_offsets, a.bone_skinning
     ref = RefBackend()
     ref.load(asset, fx)
-    consts = SimConstants(a.verts_per_strand, a.follow_per_guide)
+    # the constant block of every frame from the reference's own UpdateSimulationParameters / SetWind
+    blocks = [oracle.SimParams(), oracle.SimParams()]
     for f in range(frames):
         fin = FrameInputs(scene, f)
-        consts.update_simulation_parameters(fin.settings[0], scene.dt)
-        consts.update_bone_matrices(fin.hair_bones[0])
-        p = consts.current_params()
-        raw = (C.c_uint8 * 160).from_address(C.addressof(p))
-        fx[f"cb_header_{f}"] = np.frombuffer(bytes(raw), dtype=np.uint8).copy()
-        fx[f"cb_bones_{f}"] = p.bones_view()[:consts.num_bones].copy()
-        fx[f"cpu_iters_{f}"] = np.int32(consts.cpu_local_iterations)
-        ref.set_constants(p, consts.num_bones)
+        hdr, cpu_iters = R.update_simulation_parameters(R.settings(**fin.settings_overrides[0]), scene.dt,
+                                                        a.verts_per_strand, a.follow_per_guide, f)
+        p = blocks[f % 2]
+        C.memmove(p.header, hdr, 160)
+        bones = np.ascontiguousarray(fin.hair_bones[0], dtype=np.float32).reshape(-1, 16)
+        num_bones = min(len(bones), 512)
+        p.bones_view()[:num_bones] = bones[:num_bones]
+        fx[f"cb_header_{f}"] = np.frombuffer(hdr, dtype=np.uint8).copy()
+        fx[f"cb_bones_{f}"] = p.bones_view()[:num_bones].copy()
+        fx[f"cpu_iters_{f}"] = np.int32(cpu_iters)
+        ref.set_constants(p, num_bones)
         if o.mesh is not None:
             g = fin.grids[0]
             fx[f"mesh_bones_{f}"] = np.asarray(fin.mesh_bones[0], dtype=np.float32)
@@ -127,11 +133,10 @@ def make(name, scene, frames, stage_frames) -> dict:
             fx[f"h_skinned_{f}"] = digest(ref.mesh_skin(fx[f"mesh_bones_{f}"]))
             fx[f"h_sdf_{f}"] = digest(ref.sdf_build(g))
         for k in (1, 2, 3, 4, 5, 6):
-            for _ in range(consts.cpu_local_iterations if k == 4 else 1):
+            for _ in range(cpu_iters if k == 4 else 1):
                 ref.stage(k)
             if f in stage_frames:
                 fx[f"h_stage{k}_{f}"] = state_digest(ref.state())
-        consts.increase_simulation_frame()
         if o.mesh is not None:
             ref.collide(fin.grids[0], float(fx[f"margin_{f}"]))
         fx[f"h_end_{f}"] = state_digest(ref.state())

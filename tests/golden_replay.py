@@ -36,7 +36,7 @@ def load(name: str) -> dict:
 
 def fixtures() -> list[str]:
     """The frame-sequence fixtures (mc_*.npz hold marching-cubes cases, read by their own test)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("mc_"))
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("mc_", "sim_params_")))
 
 
 def sim_params(fx: dict, frame: int):

@@ -1,5 +1,6 @@
-"""Host-side logic of the C ABI (no device): settings defaults, the constant block written by
-UpdateSimulationParameters / SetWind, SDF grid sizing, and argument validation."""
+"""Host-side logic of the C ABI (no device): the local-iteration split and reset frames of the
+constant block (its every word, wind included, is pinned to the reference's own code by
+test_consts_pin.py), the double-buffered blocks, SDF grid sizing, and argument validation."""
 import ctypes as C
 import math
 
@@ -12,50 +13,6 @@ from tressfx_gb300.api import SimConstants, default_settings, fill_sim_params, g
 
 def f32(x):
     return np.float32(x)
-
-
-def set_wind_reference(direction, mag, frame):
-    """SetWind (TressFXHairObject.cpp:191-235) restated in float32 numpy."""
-    s = np.sin(f32(frame) * f32(0.01))
-    wM = f32(mag) * (s * s + f32(0.5))
-    d = np.asarray(direction, dtype=np.float32)
-    d = d / np.sqrt((d * d).sum())
-    xcw = np.cross(np.float32([1, 0, 0]), d).astype(np.float32)
-    ang = np.arcsin(np.sqrt((xcw * xcw).sum()))
-
-    def quat(axis, a):
-        h = f32(0.5) * f32(a)
-        return np.concatenate([np.sin(h) * np.asarray(axis, np.float32), [np.cos(h)]]).astype(np.float32)
-
-    def qmul(a, b):
-        x1, y1, z1, w1 = a
-        x2, y2, z2, w2 = b
-        return np.float32([w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2, w1 * y2 + y1 * w2 + z1 * x2 - x1 * z2,
-                           w1 * z2 + z1 * w2 + x1 * y2 - y1 * x2, w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2])
-
-    def qrot(q, v):
-        qv = q[:3]
-        uv = np.cross(qv, v)
-        uuv = np.cross(qv, uv)
-        return v + uv * (2 * q[3]) + uuv * 2
-
-    base = np.float32([0, 0, 0, 1])
-    if ang > 0.001:
-        base = quat(xcw / np.sqrt((xcw * xcw).sum()), ang)
-    cone = f32(40.0) * f32(3.14159265359) / f32(180)
-    out = []
-    for axis in ([0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]):
-        v = qrot(qmul(base, quat(axis, cone)), np.float32([1, 0, 0]))
-        out.append(v * wM)
-    return out
-
-
-def test_settings_defaults(built_lib):
-    s = default_settings()
-    assert s.vsp_coeff == f32(0.8) and s.vsp_accel_threshold == f32(1.4)
-    assert s.local_constraint_stiffness == f32(0.9) and s.local_constraints_iterations == 2
-    assert s.length_constraints_iterations == 2 and s.damping == f32(0.08)
-    assert tuple(s.wind_direction) == (1.0, 0.0, 0.0) and s.clamp_position_delta == 20.0
 
 
 @pytest.mark.parametrize("n,expect_gpu,expect_cpu", [(16, 1, 3), (32, 1, 3), (64, 3, 1)])
@@ -76,21 +33,6 @@ def test_reset_on_first_two_frames(built_lib):
         p = A.SimParams()
         fill_sim_params(p, s, 1 / 60, 16, 0, frame)
         assert p.reset_positions == want
-
-
-@pytest.mark.parametrize("direction,frame", [((1, 0, 0), 0), ((1, 0, 0.3), 17), ((0, 0, 1), 250), ((-1, 2, 0.5), 99)])
-def test_wind_corners(built_lib, direction, frame):
-    s = default_settings()
-    s.wind_magnitude = 2.0
-    for i in range(3):
-        s.wind_direction[i] = direction[i]
-    p = A.SimParams()
-    fill_sim_params(p, s, 1 / 60, 16, 0, frame)
-    want = set_wind_reference(direction, 2.0, frame)
-    for k, name in enumerate(["wind", "wind1", "wind2", "wind3"]):
-        got = np.float32(getattr(p, name)[:3])
-        assert np.allclose(got, want[k], atol=2e-6), (name, got, want[k])
-        assert getattr(p, name)[3] == 0.0
 
 
 def test_sim_constants_double_buffer(built_lib):

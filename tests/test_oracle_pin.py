@@ -38,7 +38,7 @@ def test_oracle_equals_reference_every_kernel(oracle_lib, name, scene):
         fin = FrameInputs(scene, f)
         # oracle side, stage by stage, in lock-step with the reference
         for i, c in enumerate(ora.consts):
-            c.update_simulation_parameters(fin.settings[i], scene.dt)
+            c.update_simulation_parameters(fin.settings_overrides[i], scene.dt)
             c.update_bone_matrices(fin.hair_bones[i])
         mismatches = []
 

@@ -58,7 +58,7 @@ def test_every_stage_bit_exact_from_identical_state(ctx, scene_fn):
         fin = FrameInputs(sc, f)
         gpu.prepare(fin)
         for i, c in enumerate(ora.consts):
-            c.update_simulation_parameters(fin.settings[i], sc.dt)
+            c.update_simulation_parameters(fin.settings_overrides[i], sc.dt)
             c.update_bone_matrices(fin.hair_bones[i])
         for i, o in enumerate(sc.objects):
             if o.mesh is None:

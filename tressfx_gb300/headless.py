@@ -30,19 +30,24 @@ def settings_struct(d: dict) -> A.SimSettings:
 
 
 class FrameInputs:
-    """Everything the host feeds one frame: per-object settings, hair bones, mesh bones, SDF grid."""
+    """Everything the host feeds one frame: per-object settings, hair bones, mesh bones, SDF grid.
+
+    `settings_overrides` holds each object's settings as a dict of TressFXSimulationSettings fields
+    (the scene's values with this frame's wind magnitude); `settings` turns them into the library's
+    structs on first use, so that a CPU-only consumer never loads the library."""
 
     def __init__(self, scene: Scene, frame: int):
         t = frame * scene.dt
         self.frame = frame
-        self.settings = []
+        self.settings_overrides: list[dict] = []
+        self._settings: list[A.SimSettings] | None = None
         self.hair_bones = []
         self.mesh_bones = []
         self.grids = []
         for o in scene.objects:
             st = dict(o.settings)
             st["wind_magnitude"] = wind_magnitude(scene, o, frame)
-            self.settings.append(settings_struct(st))
+            self.settings_overrides.append(st)
             self.hair_bones.append(o.bone_fn(t) if o.bone_fn is not None else np.eye(4, dtype=np.float32).reshape(1, 16))
             if o.mesh is not None:
                 mb = o.mesh_bone_fn(t)
@@ -51,6 +56,12 @@ class FrameInputs:
             else:
                 self.mesh_bones.append(None)
                 self.grids.append(None)
+
+    @property
+    def settings(self) -> list[A.SimSettings]:
+        if self._settings is None:
+            self._settings = [settings_struct(d) for d in self.settings_overrides]
+        return self._settings
 
 
 class PlainPipeline:
