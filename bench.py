@@ -3,14 +3,17 @@
 A step is one full frame of the per-frame pipeline (Simulation::StartSimulation order): skin the
 collision meshes, rebuild the SDFs, simulate every hair object, collide.  Workloads (seeded,
 synthetic):
+  batched  64 objects, strands log-uniform 512..50,000, n in {8,16,32,64}, per-object settings,
+           meshes of 5k..30k triangles and SDFs of 32^3..128^3 (24.2 M vertices)   [default]
   head     20,000 guides x 32 vertices, 4 follows per guide (3.2 M vertices), 20k-triangle head mesh
            skinned by 3 joints, SDF 64^3 rebuilt every frame, 3 local-shape + 3 length iterations,
-           VSP, wind 2 m/s with +-30 % noise                                    [default]
+           VSP, wind 2 m/s with +-30 % noise
   fur      200,000 strands x 16 vertices, 50k-triangle torso, SDF 128^3, 2 + 2 iterations
-  batched  64 objects, strands log-uniform 512..50,000, n in {8,16,32,64}, per-object settings,
-           meshes of 5k..30k triangles and SDFs of 32^3..128^3
   small    2,048 x 16, no SDF (the parity configuration)
 
+fp64   = the error of the GPU path against the FP64 oracle on the 2,048 x 16 parity workload after the
+         first dynamic frame and after 120 frames (in strand lengths), next to its error against the
+         FP32 oracle (zero: the GPU path equals it bit for bit).
 value  = vertices simulated per second over exactly --steps timed frames of the batched path (one
          CUDA-graph launch per frame), device time from CUDA events on the library's stream, inputs
          resident in HBM.  The plain path (one launch per object per stage, the reference's dispatch
@@ -55,16 +58,16 @@ WORKLOADS = {
 
 # ------------------------------------------------------------------------------------------ utils
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel, from
-# one ncu --set full capture of the same workload at frame 21 (the capture and its command are
-# summarised in profiles/k_fused_strands_k_follow_collide_head_n32.md).  ncu flushes the caches
-# before the capture and does not count writes still in L2 when the kernel ends.
+# one ncu capture of the same workload (the captures' summaries, with their commands, are kept under
+# profiles/).  ncu flushes the caches before the capture and does not count writes still in L2 when
+# the kernel ends.  These are recorded figures, not measured by this run.
 NCU_TRAFFIC = {
     ("head", "k_follow_collide (n=32)"): 105.3e6,
     ("head", "k_fused_strands (n=32)"): 48.3e6,
     # captured on the first 8 objects (5.54 M of the class's 18.69 M vertices, 684.2 MB; the kernel
     # streams each vertex's rows once, so traffic grows with the vertices): scaled to the full launch
     ("batched", "k_fused_strands (n=64)"): 2309.7e6,
-    ("fur", "k_fused_strands (n=16)"): 387.8e6,   # profiles/k_fused_strands_fur_200000x16.md
+    ("fur", "k_fused_strands (n=16)"): 387.8e6,
 }
 
 
@@ -357,6 +360,42 @@ def oracle_sample(scene, min_seconds: float, max_seconds: float, threads: int) -
             return el, done
 
 
+def fp64_error(ctx, frames: int = 120) -> dict:
+    """The oracle as the checker of the GPU path's accuracy: the plain path on the 2,048 x 16 parity
+    workload against the FP32 oracle (expected: equal bit for bit) and the FP64 oracle (the float32
+    rounding of the dynamics), after the first dynamic frame (frame 2; frames 0 and 1 reset the
+    pose) and after `frames` frames.  Errors are max |position - oracle position| over all vertices,
+    in strand lengths."""
+    from oracle.scene_driver import OraclePipeline
+    from tressfx_gb300 import _capi as A
+    from tressfx_gb300.headless import FrameInputs, PlainPipeline
+    sc = make_scene("small")
+    gpu = PlainPipeline(ctx, sc)
+    o32 = OraclePipeline(sc, np.float32)
+    o64 = OraclePipeline(sc, np.float64)
+    n = sc.objects[0].asset.verts_per_strand
+    strand = float(sc.objects[0].asset.rest_lengths.reshape(-1, n).sum(1).mean())
+    out = {"workload": WORKLOADS["small"], "unit": "strand lengths", "strand_length_m": strand}
+
+    def record(key):
+        pos = gpu.hair[0].read(A.BUF_POSITIONS)[:, :3].astype(np.float64)
+        out[key] = {"vs_fp64": float(np.abs(pos - o64.hair[0].pos[:, :3]).max()) / strand,
+                    "vs_fp32_oracle": float(np.abs(pos - o32.hair[0].pos[:, :3]).max()) / strand,
+                    "fp32_oracle_bit_exact": bool(np.array_equal(
+                        gpu.hair[0].read(A.BUF_POSITIONS).view(np.uint32), o32.hair[0].pos.view(np.uint32)))}
+
+    for f in range(frames):
+        fin = FrameInputs(sc, f)
+        gpu.step(f)
+        o32.step(fin)
+        o64.step(fin)
+        if f == 2:
+            record("after_first_dynamic_frame")
+    record(f"after_{frames}_frames")
+    gpu.close()
+    return out
+
+
 def run_reference(args) -> dict:
     scene = make_scene(args.config, args.objects)
     threads = os.cpu_count() or 1
@@ -414,6 +453,13 @@ def run_neural(args, base_cfg: dict, metric: str) -> dict:
     st = ctx.timestamps()
     q_ms = (st[-1][1] - st[0][1]) / reps
     q_tflops = qn * MLP_FLOPS / (q_ms * 1e-3) / 1e12
+    # clocks while the query repeats for about a second
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 1.2:
+            for _ in range(50):
+                nsdf.query_device(pos_ptr, qn, pose, qout.value)
+            ctx.synchronize()
     # ---- frames: grid collision vs collision through the proxy, same inputs
     inputs = [FrameInputs(scene, f) for f in range(args.warmup + args.steps)]
 
@@ -455,6 +501,7 @@ def run_neural(args, base_cfg: dict, metric: str) -> dict:
                   "contact_slack_cells": 2.0,
                   "band_fraction": float(np.mean(bands)) / V, "frames_equal_to_grid_collision": bool(same),
                   "vertices_differing": diff},
+        "clocks": dict(clocks.summary(), window="the proxy query repeated for 1.2 s"),
         "roofline": {"bound": "tensor", "kernel": "k_nsdf_query (mma.sync bf16)", "achieved": q_tflops,
                      "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": q_tflops / peaks["bf16_tflops"],
                      "traffic": None, "peak_source": peaks["source"], "queries": qn, "launch_ms": q_ms,
@@ -558,6 +605,14 @@ def run_kernels(args, base_cfg: dict) -> dict:
     mc.set_iso_level(0.0)
     ms = timed(lambda: mc.update(sdf128, g128))
     _, count = mc.read(0)
+    # clocks while the timed kernels repeat for about a second
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 1.2:
+            for _ in range(20):
+                mc.update(sdf128, g128)
+                pipe.sdfs[0].collide(h, g64, margin)
+            ctx.synchronize()
     record("marching_cubes", ms, 128 ** 3, "cells/s", 4 * 128 ** 3 + 32 * maxv, vertices=count, max_vertices=maxv,
            grid=[128, 128, 128])
     mc.close()
@@ -569,6 +624,7 @@ def run_kernels(args, base_cfg: dict) -> dict:
             "steps": reps, "warmup": 3, "ms_per_step": m["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": dict(base_cfg, l2="L2 flushed (1 GB write) before every timed launch"),
+            "clocks": dict(clocks.summary(), window="marching cubes and SDF collision repeated for 1.2 s"),
             "roofline": {"bound": "hbm", "kernel": "k_mc_count + k_mc_write", "achieved": m["gbs"],
                          "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": m["frac_of_measured_hbm"], "traffic": None,
                          "peak_source": peaks["source"]},
@@ -576,13 +632,25 @@ def run_kernels(args, base_cfg: dict) -> dict:
 
 
 # ------------------------------------------------------------------------------------------ main
+def replica_aggregate(ms_local: float, vertices_per_frame: int, world: int, dist=None) -> tuple[float, float]:
+    """Whole-job timing of N independent replicas (one per GPU, weak scaling): the slowest rank's
+    ms per frame (MAX over the gloo group), and the vertex-steps per second of all ranks together."""
+    ms = float(ms_local)
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, vertices_per_frame * world / (ms * 1e-3)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="head", choices=list(WORKLOADS))
+    ap.add_argument("--config", default="batched", choices=list(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--autotune", type=int, default=4, help="frames per candidate shape (0: defaults)")
     ap.add_argument("--no-plain", action="store_true")
@@ -636,13 +704,7 @@ def main() -> None:
     ctx = Context(local)
     b = run_batched(ctx, scene, args.steps, args.warmup, local, args.autotune)
     p = None if args.no_plain else run_plain(ctx, scene, min(args.steps, 100), args.warmup)
-    ms = b["ms_per_step"]
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = scene.vertices_per_frame * world / (ms * 1e-3)
+    ms, value = replica_aggregate(b["ms_per_step"], scene.vertices_per_frame, world, dist)
 
     if rank == 0:
         threads = os.cpu_count() or 1
@@ -657,6 +719,7 @@ def main() -> None:
         else:
             cpu["single_thread_value"] = None
             cpu["single_thread_sample"] = f"not sampled: one frame takes about {one_core:.0f} s on one thread"
+        fp64 = fp64_error(ctx)
         guide_vpf = sum(o.asset.num_guide_strands * o.asset.verts_per_strand for o in scene.objects)
         peaks = load_peaks()
         sb, fbw = strand_bytes(scene), follow_bytes(scene)
@@ -692,6 +755,7 @@ def main() -> None:
             "kernel_ms": kern,
             "kernel_gbs": gbs,
             "cpu_baseline": cpu,
+            "fp64_error": fp64,
             "clocks": dict(b["clocks"], window="the timed frames repeated for 1.2 s"),
         }
         if p is not None:

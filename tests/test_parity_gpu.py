@@ -191,19 +191,6 @@ def test_sdf_reference_grid_rule_bit_exact(ctx):
     assert (words.view(np.float32) < 1e10).sum() > 1000
 
 
-@pytest.mark.parametrize("which", ["head", "fur"])
-def test_full_size_first_frames_bit_exact(ctx, which):
-    """Full-size workloads (20k x 32 x 5 with SDF 64^3; 200k x 16 with SDF 128^3): two frames."""
-    sc = scene_head() if which == "head" else scene_fur()
-    gpu = PlainPipeline(ctx, sc)
-    ora = OraclePipeline(sc)
-    for f in range(2):
-        gpu.step(f)
-        ora.step(FrameInputs(sc, f))
-    compare_hair(gpu.hair[0], ora.hair[0], which)
-    gpu.close()
-
-
 def test_errors_are_reported(ctx):
     from tressfx_gb300.api import HairObject
     sc = scene_small(num_guides=4, n=16)
