@@ -373,10 +373,16 @@ typedef enum tfx_batch_option {
                                        a time; 2 only the gradient stage queued.  Default per class:
                                        1 with follow hairs, else 2 at n >= 64, else 0 (get_option
                                        reports the first class's)                                   */
-    TFX_BATCH_WAIT_POLLS = 6        /* polls of the strand kernel's bounded wait for a group's bulk
+    TFX_BATCH_WAIT_POLLS = 6,       /* polls of the strand kernel's bounded wait for a group's bulk
                                        copies before its block gives up and the frame reports
                                        TFX_ERR_TIMEOUT (default 2^21; 0 gives up at once, for tests
                                        of that path).  Not a launch shape: the autotuner leaves it */
+    TFX_BATCH_SDF_FORM = 7          /* the SDF construct: 1 (default) triangles binned into 8^3-cell
+                                       tiles, one block per tile with the tile's words in shared
+                                       memory, pairs skipped when an exact lower bound proves them
+                                       farther than the cell's current value (grids of at most 1024
+                                       cells per axis); 0 one warp per triangle, the reference's
+                                       per-pair atomicMin                                           */
 } tfx_batch_option;
 /* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
  * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (format
@@ -468,6 +474,13 @@ int tfx_nsdf_collide(tfx_nsdf nsdf, tfx_hair hair, tfx_sdf sdf, const tfx_sdf_gr
 /* Master FP32 parameters (tfx_nsdf_get_info's num_params floats), e.g. to save or load a network. */
 int tfx_nsdf_get_params(tfx_nsdf nsdf, float* params, size_t count);
 int tfx_nsdf_set_params(tfx_nsdf nsdf, const float* params, size_t count);
+/* The network's forward pass for queries, evaluation and collision (no reference counterpart):
+ * 1 (default) on the fifth-generation tensor cores (tcgen05.mma, accumulators in tensor memory,
+ * 128 points per tile); 0 with mma.sync (the form the training kernels use).  Both compute the same
+ * network in bf16 with fp32 accumulation; their outputs differ in the last bits (accumulation order,
+ * bias precision).  A bounded tensor-core wait that gives up is reported as TFX_ERR_TIMEOUT by the next
+ * tfx_nsdf_evaluate, or tfx_nsdf_collide with band_count. */
+int tfx_nsdf_set_inference(tfx_nsdf nsdf, int form);
 int tfx_nsdf_get_info(tfx_nsdf nsdf, int32_t* num_params, int64_t* train_samples, int64_t* eval_samples,
                       int32_t* steps);
 

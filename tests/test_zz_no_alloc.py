@@ -28,8 +28,10 @@ def _grids():
     p = m.vertices[:, :3]
     c = (p.min(0) + p.max(0)) / 2
     r = float(np.linalg.norm(p - c, axis=1).max())
-    g0, _, _ = grid_from_bbox(c - r, c + r, 40)
+    g0, _, _ = grid_from_bbox(c - r, c + r, 34)
     g0.num_cells_x, g0.num_cells_y, g0.num_cells_z = 37, 41, 39   # 59,163 cells: 3 past a multiple of 4
+    for k in range(3):                                             # the mesh's box, two cells of margin
+        g0.origin[k] = float(np.float32(c[k] - r) - np.float32(2.0) * np.float32(g0.cell_size))
     g1 = A.SdfGrid()
     C.memmove(C.byref(g1), C.byref(g0), C.sizeof(A.SdfGrid))
     g1.origin[0] = g0.origin[0] + 3.0 * g0.cell_size   # the grid follows the moved mesh
@@ -63,8 +65,7 @@ def test_static_build_matches_allocating_build_and_oracle_twice(ctx):
         want = ref.read(cells)
         assert np.array_equal(got, want), f"call {call}: {int((got != want).sum())} cells differ from tfx_sdf_update"
         skinned = mesh.read_skinned().reshape(-1, 8)
-        words = oracle.sdf_build(g, skinned, m.indices)
-        floats = (words >> np.uint32(1)) | (words << np.uint32(31))       # IFloatFlip3
+        floats = oracle.sdf_build(g, skinned, m.indices)   # Initialize + Construct + Finalize: the floats' bits
         assert np.array_equal(got.view(np.uint32), floats), \
             f"call {call}: {int((got.view(np.uint32) != floats).sum())} cells differ from the oracle"
         assert (want.view(np.float32) < 1e10).sum() > 1000, "the mesh must reach into the grid"

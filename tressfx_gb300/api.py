@@ -411,7 +411,7 @@ class Batch:
     def build(self) -> None:
         check(A.lib().tfx_batch_build(self.handle, 0), "tfx_batch_build")
 
-    EXPANDED_GRIDS, OVERLAP_SDF, SDF_BLOCK, SPLIT_SWEEPS, FOLLOW_FORM, WAIT_POLLS = 1, 2, 3, 4, 5, 6
+    EXPANDED_GRIDS, OVERLAP_SDF, SDF_BLOCK, SPLIT_SWEEPS, FOLLOW_FORM, WAIT_POLLS, SDF_FORM = 1, 2, 3, 4, 5, 6, 7
 
     def set_option(self, option: int, value: int) -> None:
         check(A.lib().tfx_batch_set_option(self.handle, option, value), "tfx_batch_set_option")
@@ -522,6 +522,10 @@ class NeuralSDF:
         check(A.lib().tfx_nsdf_evaluate(self.handle, pool, ptr(pred), ptr(tgt), ptr(w), n, C.byref(cnt)),
               "tfx_nsdf_evaluate")
         return pred[:cnt.value], tgt[:cnt.value], w[:cnt.value]
+
+    def set_inference(self, form: int) -> None:
+        """1: the forward pass on tcgen05 (default); 0: on mma.sync."""
+        check(A.lib().tfx_nsdf_set_inference(self.handle, int(form)), "tfx_nsdf_set_inference")
 
     def query_device(self, points_ptr: int, count: int, pose, out_ptr: int) -> None:
         p = (C.c_float * 3)(*[float(x) for x in pose])

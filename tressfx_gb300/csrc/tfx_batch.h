@@ -52,6 +52,8 @@ struct BatchSdf {
     long long numCells;       // X*Y*Z
     int firstTriangle;        // prefix over SDFs
     int numTriangles;
+    int firstTile;            // prefix over SDFs of the 8x8x8-cell tiles (tiled construct)
+    int tilesX, tilesY, tilesZ;
 };
 
 // Polls of k_fused_strands' bounded wait for a group's bulk copies before the block gives up.
@@ -84,6 +86,32 @@ struct SdfBatchLaunch {
     int constructThreads;
     int expand;      // some SDF keeps a corner-expanded copy: run the expansion
 };
+
+// The tiled SDF build (tfx_sdf_tiles.cu): triangles binned into 8x8x8-cell tiles, one block per tile
+// with the tile's words in shared memory, pairs culled by an exact lower bound.  A triangle whose cell
+// box spans more than SDF_BIG_TILES tiles goes to its SDF's big list, which every tile of the SDF scans,
+// so a tile list never holds more than SDF_BIG_TILES entries per triangle.
+constexpr int SDF_BIG_TILES = 8;
+constexpr int SDF_TILE_MAX_DIM = 1024;   // grid dimensions the packed cell boxes can hold
+
+struct SdfTileLaunch {
+    const BatchSdf* sdfs;
+    int nsdf, totalTris, totalTiles, blocks;
+    int* tileCount;      // [totalTiles], then bigCount [nsdf] and workCounter [1]: zeroed by one memset
+    int* bigCount;
+    int* workCounter;
+    size_t zeroBytes;
+    int* tileStart;      // [totalTiles]: exclusive prefix within its block of 1024 tiles
+    int* blockSum;       // [ceil(totalTiles / 1024)]: exclusive prefix of the block totals
+    int* list;           // [listCapacity]: triangle indices, tile by tile
+    long long listCapacity;
+    int* bigList;        // [totalTris]: SDF i's big triangles from its firstTriangle on
+    int2* triBox;        // [totalTris]: the reference's cell box of each triangle, packed 10 bits per axis
+};
+cudaError_t launch_sdf_tiles(const SdfTileLaunch& L, cudaStream_t s);
+int sdf_tile_blocks_per_sm();
+// k_batch_sdf_expand alone (after the tiled build)
+cudaError_t launch_batch_sdf_expand(const SdfBatchLaunch& L, cudaStream_t s);
 
 cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s);
 // k_local_sweep over the groups of fl (mode 1 has run on them, mode 2 runs after)

@@ -77,6 +77,10 @@ struct tfx_batch_t {
     int nmeshes = 0, totalMeshVerts = 0;
     std::vector<BatchClass> classes;
     SdfBatchLaunch sdfL{};
+    SdfTileLaunch sdfT{};           // the tiled construct's tables
+    void* tileArena = nullptr;
+    int sdfForm = 1;                // TFX_BATCH_SDF_FORM: 0 one warp per triangle, 1 tiles (when the grids allow)
+    bool tilesAvailable = false;
 
     cudaStream_t side = nullptr;             // second capture branch: mesh skinning + SDF build
     bool overlap = true;                     // capture the SDF branch on `side`
@@ -150,6 +154,7 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
     if (b->devBlock) cudaFree(b->devBlock);
     if (b->devArena) cudaFree(b->devArena);
     if (b->expandedArena) cudaFree(b->expandedArena);
+    if (b->tileArena) cudaFree(b->tileArena);
     for (auto& c : b->classes)
         if (c.items) cudaFree(c.items);
     for (auto h : b->hairs) context_release(h->ctx);
@@ -203,7 +208,8 @@ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 static void describe(tfx_batch b) {
     char buf[1024];
-    int k = snprintf(buf, sizeof(buf), "sdf construct %d threads/block;", b->sdfL.constructThreads);
+    int k = b->sdfForm == 1 ? snprintf(buf, sizeof(buf), "sdf construct on 8^3-cell tiles, %d blocks;", b->sdfT.blocks)
+                            : snprintf(buf, sizeof(buf), "sdf construct %d threads/block;", b->sdfL.constructThreads);
     for (auto& c : b->classes)
         k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d%s%s;",
                       c.n, c.vpl, c.warps, c.blocks, c.numItems, fused_group_size(c.n),
@@ -257,7 +263,13 @@ static int launch_sdf_part(tfx_batch b, cudaStream_t s) {
         if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: mesh skinning launch");
     }
     if (!b->sdfs.empty()) {
-        cudaError_t e = launch_batch_sdf(b->sdfL, s);
+        cudaError_t e;
+        if (b->sdfForm == 1) {
+            e = launch_sdf_tiles(b->sdfT, s);
+            if (e == cudaSuccess) e = launch_batch_sdf_expand(b->sdfL, s);
+        } else {
+            e = launch_batch_sdf(b->sdfL, s);
+        }
         if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: SDF launch");
     }
     return TFX_OK;
@@ -371,8 +383,12 @@ static int capture_graphs(tfx_batch b) {
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     }
-    int launches = (b->totalMeshVerts > 0 ? 1 : 0) +
-                   (b->sdfs.empty() ? 0 : (b->sdfL.totalTris > 0 ? 3 : 2) + (b->sdfL.expand ? 1 : 0));
+    int sdfLaunches = 0;
+    if (!b->sdfs.empty()) {
+        if (b->sdfForm == 1) sdfLaunches = (b->sdfT.totalTris > 0 ? 5 : 1) + (b->sdfL.expand ? 1 : 0);
+        else sdfLaunches = (b->sdfL.totalTris > 0 ? 3 : 2) + (b->sdfL.expand ? 1 : 0);
+    }
+    int launches = (b->totalMeshVerts > 0 ? 1 : 0) + sdfLaunches;
     for (auto& c : b->classes) launches += c.numItems > 0 ? (c.splitSweeps ? 4 : 2) : 0;
     b->launchesPerFrame = launches;
     return TFX_OK;
@@ -466,14 +482,21 @@ static int autotune(tfx_batch b, int frames) {
     float best = 1e30f;
     if ((rc = time_graph_frames(b, frames, &best))) { snapshot_restore(sn, s); return rc; }
     if (!b->sdfs.empty() && b->sdfL.totalTris > 0) {
-        int bestThreads = b->sdfL.constructThreads;
-        for (int th : {64, 128, 256}) {
-            if (th == bestThreads) continue;
-            b->sdfL.constructThreads = th;
-            float ms;
-            if ((rc = time_graph_frames(b, frames, &ms))) break;
-            if (ms < best) { best = ms; bestThreads = th; }
+        // the construct's form (tiles, or one warp per triangle at 64 / 128 / 256 threads per block)
+        int bestForm = b->sdfForm, bestThreads = b->sdfL.constructThreads;
+        for (int form = 0; form < 2 && rc == TFX_OK; ++form) {
+            if (form == 1 && !b->tilesAvailable) continue;
+            for (int th : {64, 128, 256}) {
+                if (form == 1 && th != 128) continue;   // the tiled form has no block-size choice
+                if (form == bestForm && (form == 1 || th == bestThreads)) continue;
+                b->sdfForm = form;
+                b->sdfL.constructThreads = th;
+                float ms;
+                if ((rc = time_graph_frames(b, frames, &ms))) break;
+                if (ms < best) { best = ms; bestForm = form; bestThreads = th; }
+            }
         }
+        b->sdfForm = bestForm;
         b->sdfL.constructThreads = bestThreads;
     }
     for (size_t ci = 0; ci < b->classes.size() && rc == TFX_OK; ++ci) {
@@ -661,8 +684,9 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
                  "tfx_batch: meshes");
 
     std::vector<BatchSdf> sdfs(nsdf);
-    long long firstQuad = 0;
+    long long firstQuad = 0, firstTile = 0;
     int firstTri = 0;
+    bool tilesOk = true;
     for (int i = 0; i < nsdf; ++i) {
         tfx_sdf s = b->sdfs[i];
         tfx_mesh m = b->sdfMesh[i];
@@ -676,8 +700,52 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         d.firstQuad = firstQuad;
         d.expanded = nullptr;     // set by apply_expand_mode
         d.firstTriangle = firstTri;
+        d.tilesX = (b->sdfDims[3 * i] + 7) / 8;
+        d.tilesY = (b->sdfDims[3 * i + 1] + 7) / 8;
+        d.tilesZ = (b->sdfDims[3 * i + 2] + 7) / 8;
+        d.firstTile = (int)firstTile;
         firstQuad += (d.numCells + 3) / 4;
         firstTri += d.numTriangles;
+        firstTile += (long long)d.tilesX * d.tilesY * d.tilesZ;
+        tilesOk = tilesOk && b->sdfDims[3 * i] <= SDF_TILE_MAX_DIM && b->sdfDims[3 * i + 1] <= SDF_TILE_MAX_DIM &&
+                  b->sdfDims[3 * i + 2] <= SDF_TILE_MAX_DIM;
+    }
+    tilesOk = tilesOk && firstTile < (1LL << 30);
+    if (nsdf > 0 && tilesOk) {
+        // tile arena: [tileCount | bigCount | workCounter] (zeroed per frame), tileStart, blockSum, list,
+        // bigList, triBox
+        const long long T = firstTile, nb = (T + 1023) / 1024, tris = std::max(firstTri, 1);
+        const long long cap = (long long)SDF_BIG_TILES * tris;
+        const size_t zeroBytes = sizeof(int) * (size_t)(T + nsdf + 1);
+        const size_t parts[6] = {zeroBytes, sizeof(int) * (size_t)T, sizeof(int) * (size_t)nb, sizeof(int) * (size_t)cap,
+                                 sizeof(int) * (size_t)tris, sizeof(int2) * (size_t)tris};
+        size_t total = 0;
+        for (size_t q : parts) total += align256(q);
+        TFX_CUDA(cudaMalloc(&b->tileArena, total), "tfx_batch: SDF tile tables");
+        TFX_CUDA(cudaMemset(b->tileArena, 0, total), "tfx_batch: clear SDF tile tables");
+        char* q = (char*)b->tileArena;
+        SdfTileLaunch& L = b->sdfT;
+        L.sdfs = b->sdfTable;
+        L.nsdf = nsdf;
+        L.totalTris = firstTri;
+        L.totalTiles = (int)T;
+        L.tileCount = (int*)q;
+        L.bigCount = L.tileCount + T;
+        L.workCounter = L.bigCount + nsdf;
+        L.zeroBytes = zeroBytes;
+        q += align256(parts[0]);
+        L.tileStart = (int*)q; q += align256(parts[1]);
+        L.blockSum = (int*)q; q += align256(parts[2]);
+        L.list = (int*)q; q += align256(parts[3]);
+        L.listCapacity = cap;
+        L.bigList = (int*)q; q += align256(parts[4]);
+        L.triBox = (int2*)q;
+        L.blocks = sdf_tile_blocks_per_sm() * b->ctx->numSMs;
+        b->tilesAvailable = true;
+        b->sdfForm = 1;
+    } else {
+        b->tilesAvailable = false;
+        b->sdfForm = 0;
     }
     if (nsdf > 0)
         TFX_CUDA(cudaMemcpy(b->sdfTable, sdfs.data(), sizeof(BatchSdf) * nsdf, cudaMemcpyHostToDevice), "tfx_batch: SDFs");
@@ -927,6 +995,13 @@ extern "C" int tfx_batch_set_option(tfx_batch b, int option, int value) {
             if (value < 0) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: wait polls %d", value);
             b->waitPolls = value;
             break;
+        case TFX_BATCH_SDF_FORM:
+            if (value != 0 && value != 1) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: SDF form %d", value);
+            if (value == 1 && !b->tilesAvailable)
+                return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: tiled SDF build needs grids of at most %d cells "
+                            "per axis", SDF_TILE_MAX_DIM);
+            b->sdfForm = value;
+            break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_set_option: unknown option %d", option);
     }
     TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
@@ -945,6 +1020,7 @@ extern "C" int tfx_batch_get_option(tfx_batch b, int option, int* value) {
         case TFX_BATCH_SPLIT_SWEEPS: *value = (!b->classes.empty() && b->classes[0].splitSweeps) ? 1 : 0; break;
         case TFX_BATCH_FOLLOW_FORM: *value = b->classes.empty() ? 0 : b->classes[0].followMode; break;
         case TFX_BATCH_WAIT_POLLS: *value = b->waitPolls; break;
+        case TFX_BATCH_SDF_FORM: *value = b->sdfForm; break;
         default: return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_get_option: unknown option %d", option);
     }
     return TFX_OK;

@@ -1143,10 +1143,15 @@ cudaError_t launch_batch_sdf(const SdfBatchLaunch& L, cudaStream_t s) {
             L.sdfs, L.nsdf, L.totalTris);
     }
     k_batch_sdf_finalize<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
-    if (L.expand) {
-        const unsigned ge = (unsigned)std::min<long long>((4 * q + 255) / 256, (long long)sm_count() * 32);
-        k_batch_sdf_expand<<<ge, 256, 0, s>>>(L.sdfs, L.nsdf, q);
-    }
+    if (L.expand) return launch_batch_sdf_expand(L, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_sdf_expand(const SdfBatchLaunch& L, cudaStream_t s) {
+    if (L.nsdf <= 0 || !L.expand) return cudaSuccess;
+    const long long q = L.totalQuads;
+    const unsigned ge = (unsigned)std::min<long long>((4 * q + 255) / 256, (long long)sm_count() * 32);
+    k_batch_sdf_expand<<<ge, 256, 0, s>>>(L.sdfs, L.nsdf, q);
     return cudaGetLastError();
 }
 

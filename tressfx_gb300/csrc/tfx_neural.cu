@@ -854,9 +854,18 @@ cudaError_t launch_collide(const CollideArgs& a, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaMemsetAsync(a.marks, 0, sizeof(uint32_t) * (size_t)((cells + 31) / 32), s);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nsdf_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
-    const long long tiles = (a.vtot + 31) / 32;
-    const int blocks = (int)std::min<long long>((tiles + QUERY_WARPS - 1) / QUERY_WARPS, sm_count() * 8);
-    k_nsdf_classify<<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(a);
+    if (a.wtc) {   // the network on the tcgen05 path
+        TcArgs t{};
+        t.wtc = a.wtc; t.fr = a.fr; t.pose = a.pose; t.pts = a.pos; t.err = a.err;
+        t.vtot = a.vtot; t.n = a.n; t.margin = a.margin; t.slackCells = a.slackCells; t.grid = a.grid;
+        t.bandList = a.bandList; t.bandCount = a.bandCount; t.marks = a.marks;
+        e = launch_classify_tc(t, s);
+        if (e != cudaSuccess) return e;
+    } else {
+        const long long tiles = (a.vtot + 31) / 32;
+        const int blocks = (int)std::min<long long>((tiles + QUERY_WARPS - 1) / QUERY_WARPS, sm_count() * 8);
+        k_nsdf_classify<<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(a);
+    }
     const unsigned gc = (unsigned)std::min<long long>((cells + 255) / 256, (long long)sm_count() * 16);
     k_gated_init<<<gc, 256, 0, s>>>(a.words, cells, a.bandCount);
     if (a.ntri > 0) k_gated_construct<<<(unsigned)std::min(( a.ntri + 7) / 8, sm_count() * 32), 256, 0, s>>>(a);

@@ -83,6 +83,47 @@ cudaError_t launch_sample(const float4* mesh, int nverts, const float* grid, con
                           cudaStream_t s);
 size_t acts_elements(int batch);
 
+// ---- the forward pass on the fifth-generation tensor cores (tcgen05, tfx_neural_tc.cu)
+// Packed weights: W1..W4 as K-major bf16 MMA operands [64 neurons][K] (K = 112 for layer 1, 80 for
+// layers 2-4, the halved bias in two extra input columns), then w5 (fp32, 64) and b5.
+constexpr int TC_K1 = KIN;
+constexpr int TC_KH = HID + 16;
+constexpr int TC_W1_BYTES = HID * TC_K1 * 2;
+constexpr int TC_WH_BYTES = HID * TC_KH * 2;
+constexpr int TC_OFF_W1 = 0;
+constexpr int TC_OFF_W2 = TC_OFF_W1 + TC_W1_BYTES;
+constexpr int TC_OFF_W3 = TC_OFF_W2 + TC_WH_BYTES;
+constexpr int TC_OFF_W4 = TC_OFF_W3 + TC_WH_BYTES;
+constexpr int TC_OFF_W5 = TC_OFF_W4 + TC_WH_BYTES;
+constexpr int TC_WBYTES = TC_OFF_W5 + (HID + 4) * 4;
+constexpr int TC_ABYTES = 128 * TC_K1 * 2;                 // the A operand of a 128-point tile
+constexpr size_t TC_SMEM = (size_t)TC_WBYTES + TC_ABYTES + 16;
+static_assert(TC_WBYTES % 16 == 0, "packed weights are staged as 16-byte words");
+enum { TC_POINTS = 0, TC_SAMPLES = 1, TC_CLASSIFY = 2 };
+
+struct TcArgs {
+    const uint8_t* wtc;
+    Frame fr;
+    Pose pose;
+    const float4* pts;           // TC_POINTS / TC_CLASSIFY: xyz of float4 records
+    const Sample* samples;       // TC_SAMPLES
+    int count;                   // TC_POINTS / TC_SAMPLES
+    float* out;
+    int* err;                    // set when a bounded wait for the tensor cores gave up
+    // TC_CLASSIFY: band selection and cell marks (as k_nsdf_classify)
+    long long vtot;
+    int n;
+    float margin, slackCells;
+    SdfGrid grid;
+    int* bandList;
+    int* bandCount;
+    uint32_t* marks;
+};
+cudaError_t launch_pack_tc(const float* params, uint8_t* wtc, cudaStream_t s);
+cudaError_t launch_query_tc(const TcArgs& a, cudaStream_t s);
+cudaError_t launch_query_samples_tc(const TcArgs& a, cudaStream_t s);
+cudaError_t launch_classify_tc(const TcArgs& a, cudaStream_t s);
+
 }  // namespace nsdf
 }  // namespace tfx
 
@@ -112,6 +153,8 @@ struct CollideArgs {
     const float4* mesh;      // skinned {pos, normal}
     const uint32_t* indices;
     int ntri;
+    const uint8_t* wtc;      // packed weights of the tensor-core forward pass, or null for mma.sync
+    int* err;
 };
 cudaError_t launch_collide(const CollideArgs& a, cudaStream_t s);
 

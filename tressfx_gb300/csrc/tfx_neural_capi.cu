@@ -27,6 +27,9 @@ struct tfx_nsdf_t {
     __nv_bfloat16* wbf = nullptr;
     float* bias = nullptr;
     float* lossSum = nullptr;
+    uint8_t* wtc = nullptr;         // packed weights of the tcgen05 forward pass
+    int* err = nullptr;             // a bounded wait of the tcgen05 forward pass gave up
+    int inference = 1;              // tfx_nsdf_set_inference: 1 tcgen05, 0 mma.sync
     nsdf::Sample* pool[2] = {nullptr, nullptr};
     int64_t poolCap[2] = {0, 0};
     int64_t poolSize[2] = {0, 0};
@@ -78,7 +81,8 @@ extern "C" int tfx_nsdf_create(tfx_context ctx, const tfx_nsdf_desc* d, tfx_nsdf
     h->slack = d->contact_slack_cells > 0.f ? d->contact_slack_cells : 1.0f;
     h->seed = d->seed ? d->seed : 1;
     const size_t pbytes = align256(sizeof(float) * nsdf::NPARAM);
-    const size_t total = 4 * pbytes + align256(sizeof(__nv_bfloat16) * nsdf::WBF_ALL) + align256(sizeof(float) * nsdf::NBIAS) + 256;
+    const size_t total = 4 * pbytes + align256(sizeof(__nv_bfloat16) * nsdf::WBF_ALL) + align256(sizeof(float) * nsdf::NBIAS) +
+                         256 + align256(nsdf::TC_WBYTES) + 256;
     cudaError_t e = cudaMalloc(&h->arena, total);
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "tfx_nsdf_create: cudaMalloc"); }
     char* p = (char*)h->arena;
@@ -88,11 +92,15 @@ extern "C" int tfx_nsdf_create(tfx_context ctx, const tfx_nsdf_desc* d, tfx_nsdf
     h->v = (float*)p; p += pbytes;
     h->wbf = (__nv_bfloat16*)p; p += align256(sizeof(__nv_bfloat16) * nsdf::WBF_ALL);
     h->bias = (float*)p; p += align256(sizeof(float) * nsdf::NBIAS);
-    h->lossSum = (float*)p;
+    h->lossSum = (float*)p; p += 256;
+    h->wtc = (uint8_t*)p; p += align256(nsdf::TC_WBYTES);
+    h->err = (int*)p;
     int r = TFX_OK;
     if ((e = cudaMemsetAsync(h->arena, 0, total, ctx->stream)) != cudaSuccess) r = cuda_fail(e, "tfx_nsdf_create: clear");
     if (!r && (e = nsdf::launch_init_params(h->params, h->seed, h->wbf, h->bias, ctx->stream)) != cudaSuccess)
         r = cuda_fail(e, "tfx_nsdf_create: init");
+    if (!r && (e = nsdf::launch_pack_tc(h->params, h->wtc, ctx->stream)) != cudaSuccess)
+        r = cuda_fail(e, "tfx_nsdf_create: pack");
     if (!r) r = nsdf_grow((void**)&h->pool[0], &h->poolCap[0], d->max_samples, sizeof(nsdf::Sample), "tfx_nsdf_create: pool");
     if (!r && d->max_eval_samples > 0)
         r = nsdf_grow((void**)&h->pool[1], &h->poolCap[1], d->max_eval_samples, sizeof(nsdf::Sample), "tfx_nsdf_create: pool");
@@ -124,6 +132,16 @@ extern "C" int tfx_nsdf_destroy(tfx_nsdf h) {
 }
 
 static nsdf::Pose pose_of(const float* p) { return nsdf::Pose{p ? p[0] : 0.f, p ? p[1] : 0.f, p ? p[2] : 0.f}; }
+
+// Reports (once) that a bounded wait of the tcgen05 forward pass gave up since the last check; the
+// caller has synchronized the stream.
+static int check_err(tfx_nsdf h) {
+    int flag = 0;
+    TFX_CUDA(cudaMemcpy(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost), "tfx_nsdf: error flag");
+    if (!flag) return TFX_OK;
+    TFX_CUDA(cudaMemset(h->err, 0, sizeof(int)), "tfx_nsdf: error flag");
+    return fail(TFX_ERR_TIMEOUT, "tfx_nsdf: a tensor-core wait gave up");
+}
 
 extern "C" int tfx_nsdf_add_samples(tfx_nsdf h, int pool, tfx_mesh mesh, tfx_sdf sdf, const tfx_sdf_grid* grid,
                                     const float* bones, int num_bones, const float pose[3], const float sphere[4],
@@ -184,6 +202,7 @@ extern "C" int tfx_nsdf_train(tfx_nsdf h, int steps, int batch, float lr, float*
         if (e == cudaSuccess) e = nsdf::launch_adam(h->params, h->grads, h->m, h->v, h->step, lrk, 1.0f, h->wbf, h->bias, s);
         if (e != cudaSuccess) return cuda_fail(e, "tfx_nsdf_train: step launch");
     }
+    if (cudaError_t e = nsdf::launch_pack_tc(h->params, h->wtc, s)) return cuda_fail(e, "tfx_nsdf_train: pack");
     if (mean_loss) {
         float l = 0.f;
         TFX_CUDA(cudaMemcpyAsync(&l, h->lossSum, sizeof(float), cudaMemcpyDeviceToHost, s), "tfx_nsdf_train: loss");
@@ -203,7 +222,14 @@ extern "C" int tfx_nsdf_evaluate(tfx_nsdf h, int pool, float* pred_cells, float*
     cudaStream_t s = h->ctx->stream;
     float* dev = nullptr;
     TFX_CUDA(cudaMalloc(&dev, sizeof(float) * n), "tfx_nsdf_evaluate: output");
-    cudaError_t e = nsdf::launch_query_samples(h->wbf, h->bias, h->fr, h->pool[pool], (int)n, dev, s);
+    cudaError_t e;
+    if (h->inference) {
+        nsdf::TcArgs t{};
+        t.wtc = h->wtc; t.fr = h->fr; t.samples = h->pool[pool]; t.count = (int)n; t.out = dev; t.err = h->err;
+        e = nsdf::launch_query_samples_tc(t, s);
+    } else {
+        e = nsdf::launch_query_samples(h->wbf, h->bias, h->fr, h->pool[pool], (int)n, dev, s);
+    }
     std::vector<nsdf::Sample> host;
     if (e == cudaSuccess && pred_cells) e = cudaMemcpyAsync(pred_cells, dev, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && (target_cells || weight)) {
@@ -213,6 +239,7 @@ extern "C" int tfx_nsdf_evaluate(tfx_nsdf h, int pool, float* pred_cells, float*
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(dev);
     if (e != cudaSuccess) return cuda_fail(e, "tfx_nsdf_evaluate");
+    if (int r = check_err(h)) return r;
     for (int64_t k = 0; k < (int64_t)host.size(); ++k) {
         if (target_cells) target_cells[k] = host[k].target;
         if (weight) weight[k] = host[k].weight;
@@ -224,8 +251,16 @@ extern "C" int tfx_nsdf_query(tfx_nsdf h, const void* points, int count, const f
     if (!h || count < 0 || (count > 0 && (!points || !out))) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_nsdf_query: bad argument");
     if (((uintptr_t)points & 15) != 0) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_nsdf_query: points not 16-byte aligned");
     TFX_CUDA(cudaSetDevice(h->ctx->device), "cudaSetDevice");
-    cudaError_t e = nsdf::launch_query(h->wbf, h->bias, h->fr, static_cast<const float4*>(points), count, pose_of(pose), out,
-                                       h->ctx->stream);
+    cudaError_t e;
+    if (h->inference) {
+        nsdf::TcArgs t{};
+        t.wtc = h->wtc; t.fr = h->fr; t.pose = pose_of(pose); t.pts = static_cast<const float4*>(points);
+        t.count = count; t.out = out; t.err = h->err;
+        e = nsdf::launch_query_tc(t, h->ctx->stream);
+    } else {
+        e = nsdf::launch_query(h->wbf, h->bias, h->fr, static_cast<const float4*>(points), count, pose_of(pose), out,
+                               h->ctx->stream);
+    }
     return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_nsdf_query launch");
 }
 
@@ -264,11 +299,14 @@ extern "C" int tfx_nsdf_collide(tfx_nsdf h, tfx_hair hair, tfx_sdf sdf, const tf
     a.bandCount = h->band_;
     a.bandList = h->band_ + 1;
     a.mesh = sdf->mesh; a.indices = sdf->idx; a.ntri = sdf->ntri;
+    a.wtc = h->inference ? h->wtc : nullptr;
+    a.err = h->err;
     cudaError_t e = nsdf::launch_collide(a, h->ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "tfx_nsdf_collide launch");
     if (band_count) {
         TFX_CUDA(cudaMemcpyAsync(band_count, h->band_, sizeof(int32_t), cudaMemcpyDeviceToHost, h->ctx->stream), "tfx_nsdf_collide");
         TFX_CUDA(cudaStreamSynchronize(h->ctx->stream), "cudaStreamSynchronize");
+        if (int r = check_err(h)) return r;
     }
     return TFX_OK;
 }
@@ -292,6 +330,7 @@ extern "C" int tfx_nsdf_set_params(tfx_nsdf h, const float* host, size_t count) 
     TFX_CUDA(cudaMemsetAsync(h->v, 0, sizeof(float) * count, s), "tfx_nsdf_set_params");
     TFX_CUDA(cudaMemsetAsync(h->wbf, 0, sizeof(__nv_bfloat16) * nsdf::WBF_ALL, s), "tfx_nsdf_set_params");
     cudaError_t e = nsdf::launch_adam(h->params, nullptr, nullptr, nullptr, 0, 0.f, 0.f, h->wbf, h->bias, s);
+    if (e == cudaSuccess) e = nsdf::launch_pack_tc(h->params, h->wtc, s);
     if (e != cudaSuccess) return cuda_fail(e, "tfx_nsdf_set_params");
     h->step = 0;
     TFX_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
@@ -305,5 +344,11 @@ extern "C" int tfx_nsdf_get_info(tfx_nsdf h, int32_t* num_params, int64_t* train
     if (train_samples) *train_samples = h->poolSize[0];
     if (eval_samples) *eval_samples = h->poolSize[1];
     if (steps) *steps = h->step;
+    return TFX_OK;
+}
+
+extern "C" int tfx_nsdf_set_inference(tfx_nsdf h, int form) {
+    if (!h || (form != 0 && form != 1)) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_nsdf_set_inference: form %d", form);
+    h->inference = form;
     return TFX_OK;
 }
