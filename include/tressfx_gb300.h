@@ -377,12 +377,13 @@ typedef enum tfx_batch_option {
                                        copies before its block gives up and the frame reports
                                        TFX_ERR_TIMEOUT (default 2^21; 0 gives up at once, for tests
                                        of that path).  Not a launch shape: the autotuner leaves it */
-    TFX_BATCH_SDF_FORM = 7          /* the SDF construct: 1 (default) triangles binned into 8^3-cell
+    TFX_BATCH_SDF_FORM = 7          /* the SDF construct: 0 (default) one warp per triangle, the
+                                       reference's per-pair atomicMin; 1 triangles binned into 8^3-cell
                                        tiles, one block per tile with the tile's words in shared
                                        memory, pairs skipped when an exact lower bound proves them
                                        farther than the cell's current value (grids of at most 1024
-                                       cells per axis); 0 one warp per triangle, the reference's
-                                       per-pair atomicMin                                           */
+                                       cells per axis).  Both give the same grid; the autotuner
+                                       times both                                                   */
 } tfx_batch_option;
 /* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
  * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (format
@@ -481,6 +482,14 @@ int tfx_nsdf_set_params(tfx_nsdf nsdf, const float* params, size_t count);
  * bias precision).  A bounded tensor-core wait that gives up is reported as TFX_ERR_TIMEOUT by the next
  * tfx_nsdf_evaluate, or tfx_nsdf_collide with band_count. */
 int tfx_nsdf_set_inference(tfx_nsdf nsdf, int form);
+/* Replaces pool `pool`'s samples with the caller's: count records of 8 floats (world x, y, z, target
+ * distance in cells, the 3 pose angles, weight), e.g. distances from an offline SDF.  Pool 0 also
+ * resets the pose range the collision trusts the network on to the samples' poses.  No counterpart
+ * in the reference. */
+int tfx_nsdf_set_samples(tfx_nsdf nsdf, int pool, const float* samples, int64_t count);
+/* The gradient of the loss with respect to the master parameters from the last training step
+ * (tfx_nsdf_get_info's num_params floats, parameter layout).  No counterpart in the reference. */
+int tfx_nsdf_get_gradients(tfx_nsdf nsdf, float* grads, size_t count);
 int tfx_nsdf_get_info(tfx_nsdf nsdf, int32_t* num_params, int64_t* train_samples, int64_t* eval_samples,
                       int32_t* steps);
 

@@ -79,6 +79,52 @@ def test_tcgen05_and_mma_sync_forward_agree(ctx):
     nsdf.close()
 
 
+def test_training_step_matches_numpy_backward(ctx):
+    """One training step on samples the test chooses: the weight and bias gradients of every layer
+    (k_nsdf_train's backward pass, k_nsdf_wgrad's sums) against a NumPy backward pass of the same bf16
+    network on the same drawn samples, the loss, and Adam's first step (k_nsdf_adam) on the GPU's own
+    gradient."""
+    from tressfx_gb300.api import NeuralSDF
+    lo, hi = np.array([-0.2, 1.3, -0.25]), np.array([0.25, 1.8, 0.2])
+    seed, pool, batch, lr = 11, 1000, 512, 1e-3
+    nsdf = NeuralSDF(ctx, lo, hi, cell_size=0.004, pose_scale=1.0 / 0.7, seed=seed, max_samples=4096, max_eval_samples=0)
+    rng = np.random.default_rng(4)
+    p = nsdf.params()
+    for a, b in ((R.P_B1, R.P_W2), (R.P_B2, R.P_W3), (R.P_B3, R.P_W4), (R.P_B4, R.P_W5)):
+        p[a:b] = rng.normal(0, 0.3, b - a)
+    p[R.P_B5] = 0.2
+    nsdf.set_params(p)
+    samples = np.zeros((pool, 8), np.float32)
+    samples[:, :3] = rng.uniform(lo, hi, (pool, 3))
+    samples[:, 3] = rng.uniform(-3.0, 3.0, pool)
+    samples[:, 4:7] = rng.uniform(-0.6, 0.6, (pool, 3))
+    samples[:, 7] = rng.uniform(0.5, 1.5, pool)
+    nsdf.set_samples(0, samples)
+    mean_loss = nsdf.train(1, batch=batch, lr=lr)
+    g_gpu = nsdf.gradients()
+    p1 = nsdf.params()
+    drawn = R.drawn_samples(seed, 1, batch, pool)
+    g_np, loss_np = R.train_gradients(p, samples[drawn], R.frame(lo, hi, 1.0 / 0.7))
+    # the forward passes differ in the hardware tanh and sine: a bf16 ulp in some activations
+    assert abs(mean_loss - loss_np / batch) < 0.02 * loss_np / batch, (mean_loss, loss_np / batch)
+    blocks = {"W1": (R.P_W1, R.P_B1), "b1": (R.P_B1, R.P_W2), "W2": (R.P_W2, R.P_B2), "b2": (R.P_B2, R.P_W3),
+              "W3": (R.P_W3, R.P_B3), "b3": (R.P_B3, R.P_W4), "W4": (R.P_W4, R.P_B4), "b4": (R.P_B4, R.P_W5),
+              "W5": (R.P_W5, R.P_B5), "b5": (R.P_B5, R.NPARAM)}
+    for name, (a, b) in blocks.items():
+        x, y = g_gpu[a:b].astype(np.float64), g_np[a:b].astype(np.float64)
+        ny = np.linalg.norm(y)
+        assert ny > 0, name
+        rel = np.linalg.norm(x - y) / ny
+        cos = float(x @ y / (np.linalg.norm(x) * ny))
+        assert rel < 0.05 and cos > 0.998, (name, rel, cos)
+    # Adam's first step at this call's learning rate (the cosine schedule at step 0 of 1)
+    f = np.float32
+    lr0 = f(lr) * (f(0.1) + f(0.45) * (f(1.0) + f(1.0)))
+    want = R.adam_first_step(p, g_gpu, lr0)
+    np.testing.assert_allclose(p1, want, rtol=2e-6, atol=1e-9)
+    nsdf.close()
+
+
 @pytest.fixture(scope="module")
 def small_proxy(ctx):
     from tressfx_gb300 import synthetic as S

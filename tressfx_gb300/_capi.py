@@ -202,6 +202,8 @@ _PROTOS = {
     "tfx_nsdf_get_params": (C.c_int, [P, P, C.c_size_t]),
     "tfx_nsdf_set_params": (C.c_int, [P, P, C.c_size_t]),
     "tfx_nsdf_set_inference": (C.c_int, [P, C.c_int]),
+    "tfx_nsdf_set_samples": (C.c_int, [P, C.c_int, P, C.c_int64]),
+    "tfx_nsdf_get_gradients": (C.c_int, [P, P, C.c_size_t]),
     "tfx_nsdf_get_info": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                     C.POINTER(C.c_int32)]),
     "tfx_batch_create": (C.c_int, [P, C.POINTER(P)]),

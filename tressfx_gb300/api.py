@@ -539,6 +539,17 @@ class NeuralSDF:
                                        C.byref(n) if band else None), "tfx_nsdf_collide")
         return n.value if band else None
 
+    def set_samples(self, pool: int, samples: np.ndarray) -> None:
+        """Replaces a pool with (count, 8) float32 records: x, y, z, target cells, 3 pose angles, weight."""
+        s = np.ascontiguousarray(samples, dtype=np.float32).reshape(-1, 8)
+        check(A.lib().tfx_nsdf_set_samples(self.handle, int(pool), ptr(s), len(s)), "tfx_nsdf_set_samples")
+
+    def gradients(self) -> np.ndarray:
+        n = self.info()[0]
+        out = np.empty(n, np.float32)
+        check(A.lib().tfx_nsdf_get_gradients(self.handle, ptr(out), n), "tfx_nsdf_get_gradients")
+        return out
+
     def params(self) -> np.ndarray:
         n = self.info()[0]
         out = np.empty(n, np.float32)

@@ -79,7 +79,7 @@ struct tfx_batch_t {
     SdfBatchLaunch sdfL{};
     SdfTileLaunch sdfT{};           // the tiled construct's tables
     void* tileArena = nullptr;
-    int sdfForm = 1;                // TFX_BATCH_SDF_FORM: 0 one warp per triangle, 1 tiles (when the grids allow)
+    int sdfForm = 0;                // TFX_BATCH_SDF_FORM: 0 one warp per triangle, 1 tiles (when the grids allow)
     bool tilesAvailable = false;
 
     cudaStream_t side = nullptr;             // second capture branch: mesh skinning + SDF build
@@ -742,7 +742,7 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         L.triBox = (int2*)q;
         L.blocks = sdf_tile_blocks_per_sm() * b->ctx->numSMs;
         b->tilesAvailable = true;
-        b->sdfForm = 1;
+        b->sdfForm = 0;   // measured faster on every workload here; the autotuner tries the tiles
     } else {
         b->tilesAvailable = false;
         b->sdfForm = 0;

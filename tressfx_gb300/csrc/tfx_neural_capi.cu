@@ -352,3 +352,37 @@ extern "C" int tfx_nsdf_set_inference(tfx_nsdf h, int form) {
     h->inference = form;
     return TFX_OK;
 }
+
+extern "C" int tfx_nsdf_set_samples(tfx_nsdf h, int pool, const float* samples, int64_t count) {
+    if (!h || (pool != 0 && pool != 1) || count < 0 || (count > 0 && !samples))
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_nsdf_set_samples: bad argument");
+    if (count > h->poolCap[pool])
+        return fail(TFX_ERR_SIZE, "tfx_nsdf_set_samples: %lld samples, pool %d holds %lld", (long long)count, pool,
+                    (long long)h->poolCap[pool]);
+    TFX_CUDA(cudaSetDevice(h->ctx->device), "cudaSetDevice");
+    if (count > 0)
+        TFX_CUDA(cudaMemcpyAsync(h->pool[pool], samples, sizeof(nsdf::Sample) * (size_t)count, cudaMemcpyHostToDevice,
+                                 h->ctx->stream), "tfx_nsdf_set_samples");
+    TFX_CUDA(cudaStreamSynchronize(h->ctx->stream), "cudaStreamSynchronize");
+    h->poolSize[pool] = count;
+    if (pool == 0) {   // the pose range the collision trusts the network on
+        for (int k = 0; k < 3; ++k) { h->poseLo[k] = 1e30f; h->poseHi[k] = -1e30f; }
+        for (int64_t i = 0; i < count; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const float a = samples[8 * i + 4 + k];
+                h->poseLo[k] = std::min(h->poseLo[k], a);
+                h->poseHi[k] = std::max(h->poseHi[k], a);
+            }
+    }
+    return TFX_OK;
+}
+
+extern "C" int tfx_nsdf_get_gradients(tfx_nsdf h, float* host, size_t count) {
+    if (!h || !host || count != (size_t)nsdf::NPARAM)
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_nsdf_get_gradients: need %d floats", nsdf::NPARAM);
+    TFX_CUDA(cudaSetDevice(h->ctx->device), "cudaSetDevice");
+    TFX_CUDA(cudaMemcpyAsync(host, h->grads, sizeof(float) * count, cudaMemcpyDeviceToHost, h->ctx->stream),
+             "tfx_nsdf_get_gradients");
+    TFX_CUDA(cudaStreamSynchronize(h->ctx->stream), "cudaStreamSynchronize");
+    return TFX_OK;
+}

@@ -358,10 +358,13 @@ static cudaError_t launch_tc(const TcArgs& a, long long total, cudaStream_t s) {
     if (total <= 0) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_nsdf_mlp_tc<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
     if (e != cudaSuccess) return e;
-    int perSM = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_nsdf_mlp_tc<MODE>, TC_M, TC_SMEM);
+    // resident blocks per SM: shared memory (each block holds the weights and one tile's operand)
+    // and tensor memory (512 columns per SM) decide it
+    int dev = 0, smemPerSM = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smemPerSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (e != cudaSuccess) return e;
-    perSM = std::max(1, std::min(perSM, 512 / TC_COLS));   // tensor memory: 512 columns per SM
+    const int perSM = std::max(1, std::min(smemPerSM / (int)(TC_SMEM + 1024), 512 / TC_COLS));
     const long long tiles = (total + TC_M - 1) / TC_M;
     const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>(tiles, (long long)perSM * sm_count()));
     k_nsdf_mlp_tc<MODE><<<blocks, TC_M, TC_SMEM, s>>>(a);
