@@ -263,11 +263,13 @@ def run_plain(ctx, scene, steps: int, warmup: int) -> dict:
             "kernel_ms": {k: float(np.sum(v)) / nfr for k, v in per.items()}, "launches_per_frame": launches}
 
 
-def run_batched(ctx, scene, steps: int, warmup: int, device: int, autotune: int) -> dict:
+def run_batched(ctx, scene, steps: int, warmup: int, device: int, autotune: int, sdf_form: int | None = None) -> dict:
     from tressfx_gb300 import _capi as A
     from tressfx_gb300.api import PinnedArray
     from tressfx_gb300.headless import BatchedPipeline, FrameInputs
     pipe = BatchedPipeline(ctx, scene, autotune_frames=autotune)
+    if sdf_form is not None:   # a fixed SDF construct form (kept with --autotune 0; the autotuner times both)
+        pipe.batch.set_option(pipe.batch.SDF_FORM, sdf_form)
     nframes = warmup + 2 * steps + 64
     inputs = [FrameInputs(scene, f) for f in range(nframes)]
     f = 0
@@ -657,6 +659,8 @@ def main() -> None:
     ap.add_argument("--objects", type=int, default=64,
                     help="--config batched: the first N objects of its seeded draw (a small case for profiling)")
     ap.add_argument("--nsdf-steps", type=int, default=24000, help="training steps of the proxy (--config neural)")
+    ap.add_argument("--sdf-form", type=int, default=None, choices=[0, 1],
+                    help="batched SDF construct: 0 one warp per triangle, 1 tiles with culling (fixed with --autotune 0)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -702,7 +706,7 @@ def main() -> None:
     from tressfx_gb300.api import Context
     scene = make_scene(args.config, args.objects)
     ctx = Context(local)
-    b = run_batched(ctx, scene, args.steps, args.warmup, local, args.autotune)
+    b = run_batched(ctx, scene, args.steps, args.warmup, local, args.autotune, args.sdf_form)
     p = None if args.no_plain else run_plain(ctx, scene, min(args.steps, 100), args.warmup)
     ms, value = replica_aggregate(b["ms_per_step"], scene.vertices_per_frame, world, dist)
 

@@ -43,6 +43,11 @@ public:
 
     tfx_mesh GetHandle() const { return m_mesh; }
     int GetFollowBone() const { return m_followBone; }
+    // The mesh as loaded (host copies): {pos.xyz, 0, normal.xyz, 0} per vertex, uint32 triangle
+    // indices, and {boneIndex[4], weight[4]} per vertex with bones as engine ids.
+    const std::vector<float>& GetBindPose() const { return m_vertices; }
+    const std::vector<uint32_t>& GetIndices() const { return m_tempIndices; }
+    const std::vector<float>& GetSkinning() const { return m_skinning; }
 
 private:
     std::vector<float> m_vertices;     // {pos.xyz, 0, normal.xyz, 0} per vertex

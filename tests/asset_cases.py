@@ -8,7 +8,7 @@ from pathlib import Path
 
 import numpy as np
 
-from asset_files import read_dump, strands, write_tfx, write_tfxbone
+from asset_files import read_dump, read_mesh_dump, strands, write_tfx, write_tfxbone
 
 ROOT = Path(__file__).resolve().parent.parent
 
@@ -62,3 +62,41 @@ def build_asset_dump(tmp: Path) -> Path:
                     str(ROOT / "tests" / "cpp" / "asset_dump.cpp"), "-o", str(exe), f"-L{pkg}", "-ltressfx_host",
                     "-ltfxgb300", f"-Wl,-rpath,{pkg}"], check=True, capture_output=True)
     return exe
+
+
+def build_mesh_dump(tmp: Path) -> Path:
+    """Compiles tests/cpp/mesh_dump.cpp against libtressfx_host.so."""
+    exe = tmp / "mesh_dump"
+    pkg = ROOT / "tressfx_gb300"
+    subprocess.run([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-ffp-contract=off", f"-I{ROOT / 'include'}",
+                    str(ROOT / "tests" / "cpp" / "mesh_dump.cpp"), "-o", str(exe), f"-L{pkg}", "-ltressfx_host",
+                    "-ltfxgb300", f"-Wl,-rpath,{pkg}"], check=True, capture_output=True)
+    return exe
+
+
+def run_mesh_driver(exe: Path, tmp: Path, mesh: Path, follow_bone: str = "b0") -> tuple[np.ndarray, dict[str, np.ndarray]]:
+    out = tmp / f"{mesh.stem}.{exe.name}.bin"
+    subprocess.run([str(exe), str(mesh), follow_bone, str(out)], check=True, capture_output=True)
+    return read_mesh_dump(out)
+
+
+# The reference's shipped asset (bin/Objects/HairAsset/Ratboy), where the reference tree is present.
+REAL_ASSET_DIR = Path(os.environ.get("TFX_REFERENCE", "/root/reference")) / "bin" / "Objects" / "HairAsset" / "Ratboy"
+# (name, .tfx, .tfxbone, follow hairs, tip separation, radius, seed)
+REAL_HAIR = ("ratboy_mohawk_f4", "Ratboy_mohawk.tfx", "Ratboy_mohawk.tfxbone", 4, 0.5, 0.012, 7)
+REAL_MESHES = ("Ratboy_body.tfxmesh", "Ratboy_left_hand.tfxmesh", "Ratboy_right_hand.tfxmesh")
+
+
+def run_real_hair(exe: Path, tmp: Path) -> tuple[np.ndarray, dict[str, np.ndarray]]:
+    name, tfx, bone, F, tip, radius, seed = REAL_HAIR
+    out = tmp / f"{name}.{exe.name}.bin"
+    subprocess.run([str(exe), str(REAL_ASSET_DIR / tfx), str(REAL_ASSET_DIR / bone), str(F), repr(tip), repr(radius),
+                    str(seed), str(out)], check=True, capture_output=True)
+    return read_dump(out)
+
+
+def mesh_digests(counts: np.ndarray, arrays: dict[str, np.ndarray]) -> dict[str, str]:
+    out = {"counts": hashlib.sha256(counts.tobytes()).hexdigest()}
+    for k, v in arrays.items():
+        out[k] = hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest()
+    return out

@@ -85,3 +85,18 @@ def read_dump(path: Path) -> tuple[np.ndarray, dict[str, np.ndarray]]:
         out[name] = np.frombuffer(raw[pos:pos + nb], dt).copy()
         pos += nb
     return counts, out
+
+
+def read_mesh_dump(path: Path) -> tuple[np.ndarray, dict[str, np.ndarray]]:
+    """(vertex count, triangle count, follow bone) and the bind pose, indices and skinning a mesh
+    dump holds (tests/cpp/mesh_dump.cpp, oracle/mesh_ref/driver.cpp)."""
+    raw = path.read_bytes()
+    counts = np.frombuffer(raw[:12], np.int32).copy()
+    pos = 12
+    out = {}
+    for name, dt in (("bind_pose", np.float32), ("indices", np.uint32), ("skinning", np.float32)):
+        (nb,) = struct.unpack_from("<Q", raw, pos)
+        pos += 8
+        out[name] = np.frombuffer(raw[pos:pos + nb], dt).copy()
+        pos += nb
+    return counts, out

@@ -1,9 +1,10 @@
-"""The C++ TressFXAsset of libtressfx_host (.tfx / .tfxbone loading, GenerateFollowHairs,
-ProcessAsset) against the reference's own TressFXAsset.cpp: array for array, bit for bit.
+"""The C++ TressFXAsset and TressFXBoneSkinning of libtressfx_host (.tfx / .tfxbone / .tfxmesh
+loading, GenerateFollowHairs, ProcessAsset) against the reference's own TressFXAsset.cpp and .tfxmesh
+parser: array for array, bit for bit.
 
-Where the reference tree is present its asset code is compiled and run beside ours
-(oracle/asset_ref); everywhere, ours is checked against the committed digests of the reference's
-output (tests/golden/asset_digests.json)."""
+Where the reference tree is present its asset code is compiled and run beside ours (oracle/asset_ref,
+oracle/mesh_ref), on synthetic files and on the reference's shipped Ratboy asset; ours is also checked
+against the committed digests of the reference's output (tests/golden/asset_digests.json)."""
 import json
 import struct
 import subprocess
@@ -12,8 +13,9 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from asset_cases import CASES, build_asset_dump, digests, run_driver, write_case_files
-from asset_files import strands, write_tfx, write_tfxbone
+from asset_cases import CASES, REAL_ASSET_DIR, REAL_HAIR, REAL_MESHES, build_asset_dump, build_mesh_dump, \
+    digests, mesh_digests, run_driver, run_mesh_driver, run_real_hair, write_case_files
+from asset_files import strands, write_tfx, write_tfxbone, write_tfxmesh
 
 HERE = Path(__file__).resolve().parent
 
@@ -104,3 +106,81 @@ def test_bad_files_are_rejected(dump_exe, tmp_path):
     write_tfxbone(bone, 200, 2, 1)   # more strands than the asset's 64 guides
     r = subprocess.run([str(dump_exe), str(good), str(bone), "0", "0", "0", "1", str(tmp_path / "o.bin")], capture_output=True)
     assert r.returncode == 4
+
+
+@pytest.fixture(scope="module")
+def mesh_dump_exe(built_lib, tmp_path_factory):
+    return build_mesh_dump(tmp_path_factory.mktemp("mesh_dump"))
+
+
+@pytest.fixture(scope="module")
+def mesh_ref_exe():
+    import oracle.mesh_ref as mesh_ref
+    try:
+        return mesh_ref.build()
+    except RuntimeError as e:  # pragma: no cover
+        pytest.skip(f"reference mesh parser not buildable: {e}")
+
+
+def _same(a: dict, b: dict) -> None:
+    for k in a:
+        x, y = a[k], b[k]
+        if k == "tangents":   # w is never set by the reference
+            x, y = x.reshape(-1, 4)[:, :3], y.reshape(-1, 4)[:, :3]
+        assert x.shape == y.shape and np.array_equal(x.view(np.uint32) if x.dtype == np.float32 else x,
+                                                     y.view(np.uint32) if y.dtype == np.float32 else y), k
+
+
+def test_real_ratboy_mohawk(dump_exe, ref_exe, tmp_path):
+    """The reference's shipped hair asset (2,228 strands of 32 vertices, padded to 2,240 guides, four
+    follow hairs each) through both loaders, and against the committed digests."""
+    if not (REAL_ASSET_DIR / REAL_HAIR[1]).exists():
+        pytest.skip("the reference's shipped asset is not present here")
+    counts, arrays = run_real_hair(dump_exe, tmp_path)
+    assert list(counts) == [11200, 358400, 32, 2240, 71680, 4]
+    want = json.loads((HERE / "golden" / "asset_digests.json").read_text())[REAL_HAIR[0]]
+    assert digests(counts, arrays) == want
+    if ref_exe is not None:
+        c2, a2 = run_real_hair(ref_exe, tmp_path)
+        assert np.array_equal(counts, c2)
+        _same(arrays, a2)
+
+
+@pytest.mark.parametrize("mesh", REAL_MESHES)
+def test_real_ratboy_collision_meshes(mesh_dump_exe, mesh_ref_exe, tmp_path, mesh):
+    """The reference's shipped collision meshes (the body: 12,909 vertices, 25,814 triangles, 86 bones)
+    through both .tfxmesh parsers, and against the committed digests."""
+    if not (REAL_ASSET_DIR / mesh).exists():
+        pytest.skip("the reference's shipped asset is not present here")
+    counts, arrays = run_mesh_driver(mesh_dump_exe, tmp_path, REAL_ASSET_DIR / mesh)
+    want = json.loads((HERE / "golden" / "asset_digests.json").read_text())[mesh]
+    assert mesh_digests(counts, arrays) == want
+    if mesh == "Ratboy_body.tfxmesh":
+        assert list(counts[:2]) == [12909, 25814]
+    if mesh_ref_exe is not None:
+        c2, a2 = run_mesh_driver(mesh_ref_exe, tmp_path, REAL_ASSET_DIR / mesh)
+        assert np.array_equal(counts, c2)
+        _same(arrays, a2)
+
+
+def test_tfxmesh_parsers_agree_on_synthetic_files(mesh_dump_exe, mesh_ref_exe, tmp_path):
+    """A synthetic .tfxmesh with comments, blank lines and bone names the scene maps to ids."""
+    if mesh_ref_exe is None:
+        pytest.skip("reference tree not present")
+    rng = np.random.default_rng(12)
+    V, T = 300, 500
+    verts = np.zeros((V, 8), np.float32)
+    verts[:, :3] = rng.normal(size=(V, 3))
+    verts[:, 4:7] = rng.normal(size=(V, 3))
+    skin = np.zeros((V, 8), np.float32)
+    skin[:, :4] = rng.integers(0, 5, (V, 4))
+    skin[:, 4:] = rng.dirichlet(np.ones(4), V)
+    idx = rng.integers(0, V, 3 * T).astype(np.uint32)
+    path = tmp_path / "synthetic.tfxmesh"
+    write_tfxmesh(path, verts, idx, skin, 5)
+    text = path.read_text().replace("numOfVertices", "\n# a comment\n\nnumOfVertices", 1)
+    path.write_text(text)
+    c1, a1 = run_mesh_driver(mesh_dump_exe, tmp_path, path, "b3")
+    c2, a2 = run_mesh_driver(mesh_ref_exe, tmp_path, path, "b3")
+    assert np.array_equal(c1, c2) and c1[2] == 3
+    _same(a1, a2)
