@@ -100,3 +100,41 @@ def read_mesh_dump(path: Path) -> tuple[np.ndarray, dict[str, np.ndarray]]:
         out[name] = np.frombuffer(raw[pos:pos + nb], dt).copy()
         pos += nb
     return counts, out
+
+
+def read_tfx_guides(path: Path) -> np.ndarray:
+    """The guide strands [num, n, 4] of a .tfx file (TressFXAsset.cpp:401-440 reads the same header)."""
+    raw = path.read_bytes()
+    _, num, n, off_pos = struct.unpack_from("<fIII", raw, 0)
+    return np.frombuffer(raw, np.float32, num * n * 4, off_pos).reshape(num, n, 4).copy()
+
+
+def read_tfxbone(path: Path) -> tuple[list[bytes], np.ndarray, np.ndarray]:
+    """Bone names (with their NUL) and per-strand (bone index [S, 4], weight [S, 4]) of a .tfxbone file
+    (TressFXAsset.cpp:442-480 reads the same layout)."""
+    raw = path.read_bytes()
+    (nb,) = struct.unpack_from("<i", raw, 0)
+    pos = 4
+    names = []
+    for _ in range(nb):
+        _, ln = struct.unpack_from("<ii", raw, pos)
+        pos += 8
+        names.append(raw[pos:pos + ln])
+        pos += ln
+    (ns,) = struct.unpack_from("<i", raw, pos)
+    pos += 4
+    rec = np.frombuffer(raw, np.dtype([("strand", "<i4"), ("pairs", [("bone", "<i4"), ("weight", "<f4")], 4)]), ns, pos)
+    return names, rec["pairs"]["bone"].copy(), rec["pairs"]["weight"].copy()
+
+
+def write_tfxbone_records(path: Path, names: list[bytes], bones: np.ndarray, weights: np.ndarray) -> None:
+    """A .tfxbone file with the given bone names and per-strand (bone index, weight) records."""
+    buf = struct.pack("<i", len(names))
+    for b, name in enumerate(names):
+        buf += struct.pack("<ii", b, len(name)) + name
+    buf += struct.pack("<i", len(bones))
+    for i in range(len(bones)):
+        buf += struct.pack("<i", i)
+        for k in range(4):
+            buf += struct.pack("<if", int(bones[i, k]), float(weights[i, k]))
+    path.write_bytes(buf)

@@ -19,7 +19,7 @@ ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
 
-from golden_replay import GOLDEN, STATE_KEYS, digest, state_digest  # noqa: E402
+from golden_replay import GOLDEN, INPUT_KEYS, STATE_KEYS, digest, state_digest  # noqa: E402
 
 
 class RefBackend:
@@ -79,8 +79,13 @@ def cases():
     small32 = S.scene_small(seed=105, num_guides=128, n=32)
     small32.objects[0].settings.update(local_constraints_iterations=2, wind_magnitude=1.0, tip_separation=0.5)
     head = S.scene_head(seed=104, num_guides=64, n=8, follows=1, triangles=1200, sdf_cells=20, frames=4)
+    # the slice of the shipped Ratboy asset (tests/golden/ratboy_subset.npz): its arrays stay in that file
+    import ratboy_scene
+    ratboy = ratboy_scene.scene(frames=5, margin_cells=0.5)
+    ratboy.meta["inputs_from"] = "ratboy_subset"
     return [("small_64x16", small16, 5, {2}), ("small_64x4", small4, 6, {2, 5}), ("small_64x64_wind", small64, 3, {2}),
-            ("small_128x32_wind", small32, 4, {3}), ("head_64x8_F1_sdf20", head, 4, {2, 3})]
+            ("small_128x32_wind", small32, 4, {3}), ("head_64x8_F1_sdf20", head, 4, {2, 3}),
+            ("real_ratboy_slice_sdf", ratboy, 5, {2, 4})]
 
 
 def make(name, scene, frames, stage_frames) -> dict:
@@ -142,6 +147,10 @@ def make(name, scene, frames, stage_frames) -> dict:
         fx[f"h_end_{f}"] = state_digest(ref.state())
     for k in STATE_KEYS:
         fx[f"final_{k}"] = ref.state()[k].copy()
+    if "inputs_from" in scene.meta:   # asset and mesh arrays are read from that fixture on replay
+        for k in INPUT_KEYS + tuple(f"final_{k}" for k in STATE_KEYS):
+            fx.pop(k, None)
+        fx["inputs_from"] = np.array(scene.meta["inputs_from"])
     return fx
 
 

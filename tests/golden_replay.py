@@ -29,14 +29,31 @@ def state_digest(st: dict) -> str:
     return digest(*[st[k] for k in STATE_KEYS])
 
 
+# arrays a fixture may take from another fixture (key "inputs_from") instead of holding them itself
+INPUT_KEYS = ("positions", "tangents", "rest_lengths", "follow_root_offsets", "bone_skinning", "mesh_vertices",
+              "mesh_indices", "mesh_skinning")
+
+
 def load(name: str) -> dict:
-    z = np.load(GOLDEN / f"{name}.npz", allow_pickle=False)
-    return {k: z[k] for k in z.files}
+    with np.load(GOLDEN / f"{name}.npz", allow_pickle=False) as z:
+        fx = {k: z[k] for k in z.files}
+    if "inputs_from" in fx:
+        with np.load(GOLDEN / f"{fx['inputs_from']}.npz", allow_pickle=False) as z:
+            for k in INPUT_KEYS:
+                fx[k] = z[k]
+        n = int(fx["counts"][1])
+        fx["positions"] = fx["positions"].reshape(-1, 4)
+        fx["tangents"] = fx["tangents"].reshape(-1, 4)
+        fx["follow_root_offsets"] = fx["follow_root_offsets"].reshape(-1, 4)
+        fx["bone_skinning"] = fx["bone_skinning"].reshape(-1, 8)
+        assert fx["positions"].shape[0] % n == 0
+    return fx
 
 
 def fixtures() -> list[str]:
-    """The frame-sequence fixtures (mc_*.npz hold marching-cubes cases, read by their own test)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("mc_", "sim_params_")))
+    """The frame-sequence fixtures (mc_*.npz hold marching-cubes cases, sim_params_*.npz constant blocks and
+    ratboy_*.npz a slice of the shipped asset, each read by its own tests)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("mc_", "sim_params_", "ratboy_")))
 
 
 def sim_params(fx: dict, frame: int):

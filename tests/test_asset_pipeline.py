@@ -15,7 +15,7 @@ import pytest
 
 from asset_cases import CASES, REAL_ASSET_DIR, REAL_HAIR, REAL_MESHES, build_asset_dump, build_mesh_dump, \
     digests, mesh_digests, run_driver, run_mesh_driver, run_real_hair, write_case_files
-from asset_files import strands, write_tfx, write_tfxbone, write_tfxmesh
+from asset_files import read_dump, strands, write_tfx, write_tfxbone, write_tfxmesh
 
 HERE = Path(__file__).resolve().parent
 
@@ -184,3 +184,24 @@ def test_tfxmesh_parsers_agree_on_synthetic_files(mesh_dump_exe, mesh_ref_exe, t
     c2, a2 = run_mesh_driver(mesh_ref_exe, tmp_path, path, "b3")
     assert np.array_equal(c1, c2) and c1[2] == 3
     _same(a1, a2)
+
+
+def test_ratboy_slice_through_library_loader(dump_exe, tmp_path):
+    """The slice of the shipped mohawk kept in tests/golden/ratboy_subset.npz (120 guides, real bone
+    records) written back to a .tfx / .tfxbone pair and loaded by the library: every array matches what
+    the reference's TressFXAsset produced from the same files (the fixture's arrays and digests)."""
+    from asset_files import write_tfxbone_records
+    with np.load(HERE / "golden" / "ratboy_subset.npz", allow_pickle=False) as z:
+        f = {k: z[k] for k in z.files}
+    F, tip, radius, seed = f["options"]
+    write_tfx(tmp_path / "slice.tfx", f["raw_guides"])
+    names = [bytes(x) + b"\0" for x in f["raw_bone_names"]]
+    write_tfxbone_records(tmp_path / "slice.tfxbone", names, f["raw_bones"], f["raw_weights"])
+    out = tmp_path / "slice.bin"
+    subprocess.run([str(dump_exe), str(tmp_path / "slice.tfx"), str(tmp_path / "slice.tfxbone"), str(int(F)), repr(float(tip)),
+                    repr(float(radius)), str(int(seed)), str(out)], check=True, capture_output=True)
+    counts, arrays = read_dump(out)
+    assert np.array_equal(counts, f["counts"])
+    assert digests(counts, arrays) == json.loads(str(f["loader_digests"]))
+    for k in ("positions", "follow_root_offsets", "rest_lengths", "bone_skinning"):
+        assert np.array_equal(arrays[k].view(np.uint32), f[k].view(np.uint32)), k

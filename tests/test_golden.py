@@ -12,4 +12,5 @@ def test_oracle_matches_reference_fixture(oracle_lib, name):
 
 def test_fixture_set_is_complete():
     names = fixtures()
-    assert {"small_64x16", "small_64x4", "small_64x64_wind", "small_128x32_wind", "head_64x8_F1_sdf20"} <= set(names)
+    assert {"small_64x16", "small_64x4", "small_64x64_wind", "small_128x32_wind", "head_64x8_F1_sdf20",
+            "real_ratboy_slice_sdf"} <= set(names)
