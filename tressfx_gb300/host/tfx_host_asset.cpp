@@ -1,5 +1,6 @@
 // TressFXAsset: .tfx / .tfxbone loading, procedural follow hairs and the derived simulation data,
 // following src/TressFX/TressFXAsset.cpp step for step (same arithmetic on the same types).
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -80,15 +81,15 @@ bool TressFXAsset::LoadHairData(FILE* ioObject) {
     EI_Seek(ioObject, (long)header.offsetVertexPosition);
     if (!read_exact(m_positions.data(), (size_t)numStrandsInFile * n * sizeof(AMD::float4), ioObject)) return false;
     // made-up strands repeat the file's last strand
-    const int numStrandsToMakeUp = m_numGuideStrands - (int)numStrandsInFile;
-    for (int i = 0; i < numStrandsToMakeUp; ++i)
+    const int padStrands = m_numGuideStrands - (int)numStrandsInFile;
+    for (int i = 0; i < padStrands; ++i)
         for (int j = 0; j < n; ++j)
             m_positions[(numStrandsInFile + i) * n + j] = m_positions[(numStrandsInFile - 1) * n + j];
 
     m_strandUV.assign(m_numTotalStrands, AMD::float2{0.0f, 0.0f});
     EI_Seek(ioObject, (long)header.offsetStrandUV);
     if (!read_exact(m_strandUV.data(), (size_t)numStrandsInFile * sizeof(AMD::float2), ioObject)) return false;
-    for (int i = 0; i < numStrandsToMakeUp; ++i) m_strandUV[numStrandsInFile + i] = m_strandUV[numStrandsInFile - 1];
+    for (int i = 0; i < padStrands; ++i) m_strandUV[numStrandsInFile + i] = m_strandUV[numStrandsInFile - 1];
 
     m_followRootOffsets.assign(m_numTotalStrands, Vector3());
     return true;
@@ -101,47 +102,50 @@ bool TressFXAsset::GenerateFollowHairs(int numFollowHairsPerGuideHair, float tip
     if (numFollowHairsPerGuideHair == 0) return false;
 
     const int n = m_numVerticesPerStrand;
-    m_numTotalStrands = m_numGuideStrands * (m_numFollowStrandsPerGuide + 1);
+    const int group = numFollowHairsPerGuideHair + 1;      // a guide and its follow strands, in that order
+    m_numTotalStrands = m_numGuideStrands * group;
     m_numTotalVertices = m_numTotalStrands * n;
 
-    const std::vector<Vector3> positionsGuide = m_positions;
-    const std::vector<AMD::float2> strandUVGuide = m_strandUV;
+    std::vector<Vector3> guides;
+    std::vector<AMD::float2> guideUV;
+    guides.swap(m_positions);
+    guideUV.swap(m_strandUV);
     m_positions.assign(m_numTotalVertices, Vector3());
     m_strandUV.assign(m_numTotalStrands, AMD::float2{0.0f, 0.0f});
     m_followRootOffsets.assign(m_numTotalStrands, Vector3());
 
-    Vector3* pos = m_positions.data();
-    Vector3* followOffset = m_followRootOffsets.data();
-    for (int i = 0; i < m_numGuideStrands; i++) {
-        const int indexGuideStrand = i * (m_numFollowStrandsPerGuide + 1);
-        const int indexRootVertMaster = indexGuideStrand * n;
-        std::memcpy(&pos[indexRootVertMaster], &positionsGuide[(size_t)i * n], sizeof(Vector3) * n);
-        m_strandUV[indexGuideStrand] = strandUVGuide[i];
+    // a follow strand's offset from its guide grows linearly along the strand, from 1x at the root
+    std::vector<float> spread(n);
+    for (int k = 0; k < n; ++k) spread[k] = tipSeparationFactor * ((float)k / ((float)n)) + 1.0f;
 
-        followOffset[indexGuideStrand].Set(0, 0, 0);
-        followOffset[indexGuideStrand].w = (float)indexGuideStrand;
-        Vector3 v01 = pos[indexRootVertMaster + 1] - pos[indexRootVertMaster];
-        v01.Normalize();
-        Vector3 t0, t1;
-        tangent_vectors(v01, t0, t1);
+    for (int g = 0; g < m_numGuideStrands; ++g) {
+        const int lead = g * group;                         // the guide's strand index in the output
+        const Vector3* src = &guides[(size_t)g * n];
+        Vector3* guide = &m_positions[(size_t)lead * n];
+        std::copy(src, src + n, guide);
+        m_strandUV[lead] = guideUV[g];
+        m_followRootOffsets[lead] = Vector3(0.0f, 0.0f, 0.0f, (float)lead);
 
-        for (int j = 0; j < m_numFollowStrandsPerGuide; j++) {
-            const int indexStrandFollow = indexGuideStrand + j + 1;
-            const int indexRootVertFollow = indexStrandFollow * n;
-            m_strandUV[indexStrandFollow] = m_strandUV[indexGuideStrand];
-            // offset = r0 * t0 + r1 * t1.  The reference writes both draws in one expression, which
-            // leaves their order to the compiler; g++ draws the t1 coefficient first, and so does this.
-            const float r1 = GetRandom(-maxRadiusAroundGuideHair, maxRadiusAroundGuideHair);
-            const float r0 = GetRandom(-maxRadiusAroundGuideHair, maxRadiusAroundGuideHair);
-            const Vector3 offset = r0 * t0 + r1 * t1;
-            followOffset[indexStrandFollow] = offset;
-            followOffset[indexStrandFollow].w = (float)indexGuideStrand;
-            for (int k = 0; k < n; k++) {
-                const Vector3& guideVert = pos[indexRootVertMaster + k];
-                Vector3& followVert = pos[indexRootVertFollow + k];
-                const float factor = tipSeparationFactor * ((float)k / ((float)n)) + 1.0f;
-                followVert = guideVert + offset * factor;
-                followVert.w = guideVert.w;
+        // the plane of root offsets: normal to the guide's first segment
+        Vector3 axis = guide[1] - guide[0];
+        axis.Normalize();
+        Vector3 u, v;
+        tangent_vectors(axis, u, v);
+
+        for (int f = 1; f < group; ++f) {
+            const int s = lead + f;
+            m_strandUV[s] = m_strandUV[lead];
+            // The reference forms the offset from two draws in one expression, which leaves their order
+            // to the compiler; g++ draws the coefficient of the second direction first, and so does this.
+            const float cv = GetRandom(-maxRadiusAroundGuideHair, maxRadiusAroundGuideHair);
+            const float cu = GetRandom(-maxRadiusAroundGuideHair, maxRadiusAroundGuideHair);
+            const Vector3 offset = cu * u + cv * v;
+            m_followRootOffsets[s] = offset;
+            m_followRootOffsets[s].w = (float)lead;
+            Vector3* follow = &m_positions[(size_t)s * n];
+            for (int k = 0; k < n; ++k) {
+                follow[k] = guide[k] + offset * spread[k];
+                follow[k].w = guide[k].w;                   // the inverse mass is the guide's
             }
         }
     }
@@ -162,120 +166,110 @@ bool TressFXAsset::ProcessAsset() {
     return true;
 }
 
+// Two triangles per segment over the expanded vertex pairs (vertex v of the strands expands to 2v and
+// 2v + 1, TressFXAsset.cpp:392-399).
 void TressFXAsset::FillTriangleIndexArray() {
-    AMD::int32 id = 0;
-    int iCount = 0;
-    for (int i = 0; i < m_numTotalStrands; i++) {
-        for (int j = 0; j < m_numVerticesPerStrand - 1; j++) {
-            m_triangleIndices[iCount++] = 2 * id;
-            m_triangleIndices[iCount++] = 2 * id + 1;
-            m_triangleIndices[iCount++] = 2 * id + 2;
-            m_triangleIndices[iCount++] = 2 * id + 2;
-            m_triangleIndices[iCount++] = 2 * id + 1;
-            m_triangleIndices[iCount++] = 2 * id + 3;
-            id++;
+    const int n = m_numVerticesPerStrand;
+    AMD::int32* out = m_triangleIndices.data();
+    for (int s = 0; s < m_numTotalStrands; ++s)
+        for (int j = 0; j + 1 < n; ++j) {
+            const AMD::int32 a = 2 * (s * n + j);
+            const AMD::int32 quad[6] = {a, a + 1, a + 2, a + 2, a + 1, a + 3};
+            out = std::copy(quad, quad + 6, out);
         }
-        id++;
-    }
 }
 
-// ComputeStrandTangent (TressFXAsset.cpp:294-332): vertex 0 along the first segment, inner vertices
-// along the sum of the two unit segment directions, the last vertex left at zero.
+// Tangents (TressFXAsset.cpp:294-332): the root along its segment, an inner vertex along the sum of the
+// unit directions of its two segments, the tip left at zero.
 void TressFXAsset::ComputeStrandTangent() {
     const int n = m_numVerticesPerStrand;
-    auto store = [&](int idx, const Vector3& t) { m_tangents[idx] = AMD::float4{t.x, t.y, t.z, t.w}; };
-    for (int iStrand = 0; iStrand < m_numTotalStrands; ++iStrand) {
-        const int root = iStrand * n;
-        {
-            Vector3 tangent = m_positions[root + 1] - m_positions[root];
-            tangent.Normalize();
-            store(root, tangent);
-        }
-        for (int i = 1; i < n - 1; i++) {
-            Vector3 pre = m_positions[root + i] - m_positions[root + i - 1];
-            pre.Normalize();
-            Vector3 next = m_positions[root + i + 1] - m_positions[root + i];
-            next.Normalize();
-            Vector3 tangent = pre + next;
-            tangent = tangent.Normalize();
-            store(root + i, tangent);
+    auto dir = [](const Vector3& from, const Vector3& to) {
+        Vector3 d = to - from;
+        d.Normalize();
+        return d;
+    };
+    for (int s = 0; s < m_numTotalStrands; ++s) {
+        const Vector3* p = &m_positions[(size_t)s * n];
+        AMD::float4* t = &m_tangents[(size_t)s * n];
+        const Vector3 root = dir(p[0], p[1]);
+        t[0] = AMD::float4{root.x, root.y, root.z, root.w};
+        for (int i = 1; i + 1 < n; ++i) {
+            Vector3 sum = dir(p[i - 1], p[i]) + dir(p[i], p[i + 1]);
+            sum.Normalize();
+            t[i] = AMD::float4{sum.x, sum.y, sum.z, sum.w};
         }
     }
 }
 
-// ComputeThicknessCoeffs (TressFXAsset.cpp:334-364), including its running division of the strand
-// length.
+// Thickness coefficients (TressFXAsset.cpp:334-364).  The reference divides a running value, first the
+// strand length L, by L once per vertex, so vertex k gets sqrt(1 - r^2) with r = L^-k (in float); kept as
+// it is, since renderers read these values.
 void TressFXAsset::ComputeThicknessCoeffs() {
     const int n = m_numVerticesPerStrand;
-    int index = 0;
-    for (int iStrand = 0; iStrand < m_numTotalStrands; ++iStrand) {
-        const int root = iStrand * n;
-        float strandLength = 0;
-        float tVal = 0;
-        for (int i = 1; i < n; ++i) {
-            const Vector3 vec = m_positions[root + i] - m_positions[root + i - 1];
-            const float disSeg = vec.Length();
-            tVal += disSeg;
-            strandLength += disSeg;
-        }
+    for (int s = 0; s < m_numTotalStrands; ++s) {
+        const Vector3* p = &m_positions[(size_t)s * n];
+        float length = 0;
+        for (int i = 1; i < n; ++i) length += (p[i] - p[i - 1]).Length();
+        float ratio = length;
+        float* out = &m_thicknessCoeffs[(size_t)s * n];
         for (int i = 0; i < n; ++i) {
-            tVal /= strandLength;
-            m_thicknessCoeffs[index++] = sqrtf(1.f - tVal * tVal);
+            ratio /= length;
+            out[i] = sqrtf(1.f - ratio * ratio);
         }
     }
 }
 
-// ComputeRestLengths (TressFXAsset.cpp:366-390): |p_j - p_{j+1}|, 0 for the last vertex.
+// Rest lengths (TressFXAsset.cpp:366-390): the length of the segment after each vertex, 0 at the tip.
 void TressFXAsset::ComputeRestLengths() {
     const int n = m_numVerticesPerStrand;
-    int index = 0;
-    for (int i = 0; i < m_numTotalStrands; i++) {
-        const int root = i * n;
-        for (int j = 0; j < n - 1; j++) m_restLengths[index++] = (m_positions[root + j] - m_positions[root + j + 1]).Length();
-        m_restLengths[index++] = 0;
+    for (int s = 0; s < m_numTotalStrands; ++s) {
+        const Vector3* p = &m_positions[(size_t)s * n];
+        float* out = &m_restLengths[(size_t)s * n];
+        for (int j = 0; j + 1 < n; ++j) out[j] = (p[j] - p[j + 1]).Length();
+        out[n - 1] = 0;
     }
 }
 
 bool TressFXAsset::LoadBoneData(FILE* ioObject, int skinNumber, EI_Scene* scene) {
     m_boneSkinningData.clear();
     if (!ioObject || !scene) return false;
-    AMD::int32 numOfBones = 0;
+    AMD::int32 boneCount = 0;
     EI_Seek(ioObject, 0);
-    if (!read_exact(&numOfBones, sizeof(numOfBones), ioObject) || numOfBones < 0) return false;
+    if (!read_exact(&boneCount, sizeof(boneCount), ioObject) || boneCount < 0) return false;
 
-    std::vector<int> boneEngineIds(numOfBones);
-    for (int i = 0; i < numOfBones; i++) {
+    std::vector<int> engineId(boneCount);
+    for (int i = 0; i < boneCount; i++) {
         AMD::int32 boneIndex = 0, charLen = 0;
         if (!read_exact(&boneIndex, sizeof(boneIndex), ioObject)) return false;
         if (!read_exact(&charLen, sizeof(charLen), ioObject) || charLen < 0 || charLen > 128) return false;
         char boneName[129] = {};
         if (!read_exact(boneName, (size_t)charLen, ioObject)) return false;
-        boneEngineIds[i] = scene->GetBoneIdByName(skinNumber, boneName);
+        engineId[i] = scene->GetBoneIdByName(skinNumber, boneName);
     }
 
-    AMD::int32 numOfStrandsInStream = 0;
-    if (!read_exact(&numOfStrandsInStream, sizeof(numOfStrandsInStream), ioObject)) return false;
-    if (m_numGuideStrands < numOfStrandsInStream || numOfStrandsInStream <= 0) return false;
+    AMD::int32 recordCount = 0;
+    if (!read_exact(&recordCount, sizeof(recordCount), ioObject)) return false;
+    if (m_numGuideStrands < recordCount || recordCount <= 0) return false;
 
     m_boneSkinningData.assign(m_numTotalStrands, TressFXBoneSkinningData{{0, 0, 0, 0}, {0, 0, 0, 0}});
-    TressFXBoneSkinningData skinData{{0, 0, 0, 0}, {0, 0, 0, 0}};
-    for (int i = 0; i < numOfStrandsInStream; ++i) {
+    TressFXBoneSkinningData record{{0, 0, 0, 0}, {0, 0, 0, 0}};
+    for (int i = 0; i < recordCount; ++i) {
         AMD::int32 index = 0;
         if (!read_exact(&index, sizeof(index), ioObject)) return false;
         for (int j = 0; j < TRESSFX_MAX_INFLUENTIAL_BONE_COUNT; ++j) {
             AMD::int32 boneIndex = 0;
             if (!read_exact(&boneIndex, sizeof(boneIndex), ioObject)) return false;
-            if (boneIndex < 0 || boneIndex >= numOfBones) return false;
-            skinData.boneIndex[j] = (float)boneEngineIds[boneIndex];
-            if (!read_exact(&skinData.weight[j], sizeof(float), ioObject)) return false;
+            if (boneIndex < 0 || boneIndex >= boneCount) return false;
+            record.boneIndex[j] = (float)engineId[boneIndex];
+            if (!read_exact(&record.weight[j], sizeof(float), ioObject)) return false;
         }
         // an index of -1 (no bone) becomes 0; its weight is zero
         for (int j = 0; j < TRESSFX_MAX_INFLUENTIAL_BONE_COUNT; ++j)
-            skinData.boneIndex[j] = skinData.boneIndex[j] == -1.f ? 0 : skinData.boneIndex[j];
-        m_boneSkinningData[(size_t)i * (m_numFollowStrandsPerGuide + 1)] = skinData;
+            record.boneIndex[j] = record.boneIndex[j] == -1.f ? 0 : record.boneIndex[j];
+        m_boneSkinningData[(size_t)i * (m_numFollowStrandsPerGuide + 1)] = record;
     }
     // made-up guide strands take the last strand's skinning
-    for (int i = numOfStrandsInStream; i < m_numGuideStrands; ++i)
-        m_boneSkinningData[(size_t)i * (m_numFollowStrandsPerGuide + 1)] = skinData;
+    for (int i = recordCount; i < m_numGuideStrands; ++i)
+        m_boneSkinningData[(size_t)i * (m_numFollowStrandsPerGuide + 1)] = record;
     return true;
 }
