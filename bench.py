@@ -443,17 +443,23 @@ def run_neural(args, base_cfg: dict, metric: str) -> dict:
     qout = C.c_void_p()
     assert A.lib().tfx_sdf_get_buffer(scratch.handle, C.byref(qout), None) == 0
     pose = scene.meta["pose_fn"](0.0)
-    for _ in range(3):
-        nsdf.query_device(pos_ptr, qn, pose, qout.value)
-    ctx.synchronize()
-    ctx.timestamps()
-    ctx.timestamp("q0")
-    reps = 20
-    for _ in range(reps):
-        nsdf.query_device(pos_ptr, qn, pose, qout.value)
-    ctx.timestamp("q1")
-    st = ctx.timestamps()
-    q_ms = (st[-1][1] - st[0][1]) / reps
+
+    def query_ms(form: int) -> float:
+        nsdf.set_inference(form)
+        for _ in range(3):
+            nsdf.query_device(pos_ptr, qn, pose, qout.value)
+        ctx.synchronize()
+        ctx.timestamps()
+        ctx.timestamp("q0")
+        reps = 20
+        for _ in range(reps):
+            nsdf.query_device(pos_ptr, qn, pose, qout.value)
+        ctx.timestamp("q1")
+        st = ctx.timestamps()
+        return (st[-1][1] - st[0][1]) / reps
+
+    mma_ms = query_ms(0)            # warp-level mma.sync form
+    q_ms = query_ms(1)              # tcgen05 form (the default)
     q_tflops = qn * MLP_FLOPS / (q_ms * 1e-3) / 1e12
     # clocks while the query repeats for about a second
     with ClockSampler(0) as clocks:
@@ -504,7 +510,8 @@ def run_neural(args, base_cfg: dict, metric: str) -> dict:
                   "band_fraction": float(np.mean(bands)) / V, "frames_equal_to_grid_collision": bool(same),
                   "vertices_differing": diff},
         "clocks": dict(clocks.summary(), window="the proxy query repeated for 1.2 s"),
-        "roofline": {"bound": "tensor", "kernel": "k_nsdf_query (mma.sync bf16)", "achieved": q_tflops,
+        "query_forms_ms": {"tcgen05": q_ms, "mma_sync": mma_ms, "points": qn},
+        "roofline": {"bound": "tensor", "kernel": "k_nsdf_mlp_tc (tcgen05 bf16)", "achieved": q_tflops,
                      "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": q_tflops / peaks["bf16_tflops"],
                      "traffic": None, "peak_source": peaks["source"], "queries": qn, "launch_ms": q_ms,
                      "flops_per_query": MLP_FLOPS},

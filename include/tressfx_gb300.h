@@ -378,12 +378,13 @@ typedef enum tfx_batch_option {
                                        TFX_ERR_TIMEOUT (default 2^21; 0 gives up at once, for tests
                                        of that path).  Not a launch shape: the autotuner leaves it */
     TFX_BATCH_SDF_FORM = 7          /* the SDF construct: 0 (default) one warp per triangle, the
-                                       reference's per-pair atomicMin; 1 triangles binned into 8^3-cell
-                                       tiles, one block per tile with the tile's words in shared
-                                       memory, pairs skipped when an exact lower bound proves them
-                                       farther than the cell's current value (grids of at most 1024
-                                       cells per axis).  Both give the same grid; the autotuner
-                                       times both                                                   */
+                                       reference's per-pair atomicMin; 1 triangles binned into
+                                       8x8x4-cell tiles, one block per tile with the tile's words in
+                                       shared memory, a warp per 4x4x2-cell brick walking its
+                                       triangles nearest first, pairs skipped when an exact lower
+                                       bound proves them farther than the cell's current value (grids
+                                       of at most 1024 cells per axis).  Both give the same grid; the
+                                       autotuner times both                                         */
 } tfx_batch_option;
 /* The positions of every hair object (in tfx_batch_add_hair order) as they stand after the frames
  * queued so far, copied into host memory: host_dst[i] receives num_vertices * 16 bytes (format

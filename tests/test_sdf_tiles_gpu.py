@@ -1,4 +1,4 @@
-"""The batched SDF build, in both forms (TFX_BATCH_SDF_FORM 1: triangles binned into 8^3-cell tiles
+"""The batched SDF build, in both forms (TFX_BATCH_SDF_FORM 1: triangles binned into 8x8x4-cell tiles
 with exact pair culling; 0: one warp per triangle), bit for bit against the oracle's
 Initialize + Construct + Finalize on meshes chosen to break a culled construct: random soups, the
 same far from the origin, slivers, exact duplicates and coplanar overlaps (ties), tiny triangles,

@@ -52,7 +52,7 @@ struct BatchSdf {
     long long numCells;       // X*Y*Z
     int firstTriangle;        // prefix over SDFs
     int numTriangles;
-    int firstTile;            // prefix over SDFs of the 8x8x8-cell tiles (tiled construct)
+    int firstTile;            // prefix over SDFs of the 8x8x4-cell tiles (tiled construct)
     int tilesX, tilesY, tilesZ;
 };
 
@@ -87,11 +87,13 @@ struct SdfBatchLaunch {
     int expand;      // some SDF keeps a corner-expanded copy: run the expansion
 };
 
-// The tiled SDF build (tfx_sdf_tiles.cu): triangles binned into 8x8x8-cell tiles, one block per tile
+// The tiled SDF build (tfx_sdf_tiles.cu): triangles binned into 8x8x4-cell tiles, one block per tile
 // with the tile's words in shared memory, pairs culled by an exact lower bound.  A triangle whose cell
 // box spans more than SDF_BIG_TILES tiles goes to its SDF's big list, which every tile of the SDF scans,
 // so a tile list never holds more than SDF_BIG_TILES entries per triangle.
-constexpr int SDF_BIG_TILES = 8;
+constexpr int SDF_BIG_TILES = 16;
+constexpr int SDF_TILE_X = 8, SDF_TILE_Y = 8, SDF_TILE_Z = 4;
+constexpr int SDF_TRI_RECORD = 20;       // floats of a triangle's record (vertices, bound terms, cell box)
 constexpr int SDF_TILE_MAX_DIM = 1024;   // grid dimensions the packed cell boxes can hold
 
 struct SdfTileLaunch {
@@ -106,7 +108,7 @@ struct SdfTileLaunch {
     int* list;           // [listCapacity]: triangle indices, tile by tile
     long long listCapacity;
     int* bigList;        // [totalTris]: SDF i's big triangles from its firstTriangle on
-    int2* triBox;        // [totalTris]: the reference's cell box of each triangle, packed 10 bits per axis
+    float* records;      // [totalTris * SDF_TRI_RECORD]: each triangle's record, written by the binning
 };
 cudaError_t launch_sdf_tiles(const SdfTileLaunch& L, cudaStream_t s);
 int sdf_tile_blocks_per_sm();

@@ -208,7 +208,7 @@ static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 static void describe(tfx_batch b) {
     char buf[1024];
-    int k = b->sdfForm == 1 ? snprintf(buf, sizeof(buf), "sdf construct on 8^3-cell tiles, %d blocks;", b->sdfT.blocks)
+    int k = b->sdfForm == 1 ? snprintf(buf, sizeof(buf), "sdf construct on 8x8x4-cell tiles (a warp per 4x4x2 brick), %d blocks;", b->sdfT.blocks)
                             : snprintf(buf, sizeof(buf), "sdf construct %d threads/block;", b->sdfL.constructThreads);
     for (auto& c : b->classes)
         k += snprintf(buf + k, sizeof(buf) - k, " n=%d: %d vertices/lane, %d warps/block, %d blocks, %d groups of %d%s%s;",
@@ -700,9 +700,9 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         d.firstQuad = firstQuad;
         d.expanded = nullptr;     // set by apply_expand_mode
         d.firstTriangle = firstTri;
-        d.tilesX = (b->sdfDims[3 * i] + 7) / 8;
-        d.tilesY = (b->sdfDims[3 * i + 1] + 7) / 8;
-        d.tilesZ = (b->sdfDims[3 * i + 2] + 7) / 8;
+        d.tilesX = (b->sdfDims[3 * i] + SDF_TILE_X - 1) / SDF_TILE_X;
+        d.tilesY = (b->sdfDims[3 * i + 1] + SDF_TILE_Y - 1) / SDF_TILE_Y;
+        d.tilesZ = (b->sdfDims[3 * i + 2] + SDF_TILE_Z - 1) / SDF_TILE_Z;
         d.firstTile = (int)firstTile;
         firstQuad += (d.numCells + 3) / 4;
         firstTri += d.numTriangles;
@@ -713,12 +713,12 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
     tilesOk = tilesOk && firstTile < (1LL << 30);
     if (nsdf > 0 && tilesOk) {
         // tile arena: [tileCount | bigCount | workCounter] (zeroed per frame), tileStart, blockSum, list,
-        // bigList, triBox
+        // bigList, records
         const long long T = firstTile, nb = (T + 1023) / 1024, tris = std::max(firstTri, 1);
         const long long cap = (long long)SDF_BIG_TILES * tris;
         const size_t zeroBytes = sizeof(int) * (size_t)(T + nsdf + 1);
         const size_t parts[6] = {zeroBytes, sizeof(int) * (size_t)T, sizeof(int) * (size_t)nb, sizeof(int) * (size_t)cap,
-                                 sizeof(int) * (size_t)tris, sizeof(int2) * (size_t)tris};
+                                 sizeof(int) * (size_t)tris, sizeof(float) * SDF_TRI_RECORD * (size_t)tris};
         size_t total = 0;
         for (size_t q : parts) total += align256(q);
         TFX_CUDA(cudaMalloc(&b->tileArena, total), "tfx_batch: SDF tile tables");
@@ -739,7 +739,7 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         L.list = (int*)q; q += align256(parts[3]);
         L.listCapacity = cap;
         L.bigList = (int*)q; q += align256(parts[4]);
-        L.triBox = (int2*)q;
+        L.records = (float*)q;
         L.blocks = sdf_tile_blocks_per_sm() * b->ctx->numSMs;
         b->tilesAvailable = true;
         b->sdfForm = 0;   // measured faster on every workload here; the autotuner tries the tiles

@@ -95,9 +95,14 @@ constexpr int TC_OFF_W2 = TC_OFF_W1 + TC_W1_BYTES;
 constexpr int TC_OFF_W3 = TC_OFF_W2 + TC_WH_BYTES;
 constexpr int TC_OFF_W4 = TC_OFF_W3 + TC_WH_BYTES;
 constexpr int TC_OFF_W5 = TC_OFF_W4 + TC_WH_BYTES;
-constexpr int TC_WBYTES = TC_OFF_W5 + (HID + 4) * 4;
+constexpr int TC_N5 = 16;                                  // output layer as an N = 16 MMA (column 0 used)
+constexpr int TC_OFF_B5 = TC_OFF_W5 + TC_N5 * TC_KH * 2;   // b5 (fp32), then padding to 16 bytes
+constexpr int TC_WBYTES = TC_OFF_B5 + 16;
 constexpr int TC_ABYTES = 128 * TC_K1 * 2;                 // the A operand of a 128-point tile
-constexpr size_t TC_SMEM = (size_t)TC_WBYTES + TC_ABYTES + 16;
+constexpr int TC_NWG = 5;                                  // warpgroups (tiles in flight) per block
+// weights once per block, one A operand per warpgroup, then an mbarrier per warpgroup and the
+// tensor-memory address slot
+constexpr size_t TC_SMEM = (size_t)TC_WBYTES + (size_t)TC_NWG * TC_ABYTES + 8 * TC_NWG + 16;
 static_assert(TC_WBYTES % 16 == 0, "packed weights are staged as 16-byte words");
 enum { TC_POINTS = 0, TC_SAMPLES = 1, TC_CLASSIFY = 2 };
 
