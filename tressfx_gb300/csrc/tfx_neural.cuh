@@ -98,11 +98,10 @@ constexpr int TC_OFF_W5 = TC_OFF_W4 + TC_WH_BYTES;
 constexpr int TC_N5 = 16;                                  // output layer as an N = 16 MMA (column 0 used)
 constexpr int TC_OFF_B5 = TC_OFF_W5 + TC_N5 * TC_KH * 2;   // b5 (fp32), then padding to 16 bytes
 constexpr int TC_WBYTES = TC_OFF_B5 + 16;
-constexpr int TC_ABYTES = 128 * TC_K1 * 2;                 // the A operand of a 128-point tile
-constexpr int TC_NWG = 5;                                  // warpgroups (tiles in flight) per block
-// weights once per block, one A operand per warpgroup, then an mbarrier per warpgroup and the
-// tensor-memory address slot
-constexpr size_t TC_SMEM = (size_t)TC_WBYTES + (size_t)TC_NWG * TC_ABYTES + 8 * TC_NWG + 16;
+constexpr int TC_NWG = 4;                                  // warpgroups (tiles in flight) per block
+// shared memory: the weights once per block, then an mbarrier per warpgroup and the tensor-memory
+// address slot (the A operands and accumulators live in tensor memory)
+constexpr size_t TC_SMEM = (size_t)TC_WBYTES + 8 * TC_NWG + 16;
 static_assert(TC_WBYTES % 16 == 0, "packed weights are staged as 16-byte words");
 enum { TC_POINTS = 0, TC_SAMPLES = 1, TC_CLASSIFY = 2 };
 

@@ -2,20 +2,21 @@
 //
 // A block holds the packed weights once in shared memory and runs TC_NWG warpgroups, each carrying
 // its own tiles of 128 points through the network, so that one warpgroup's feature and activation
-// arithmetic overlaps the other warpgroups' MMAs.  In a warpgroup, thread r computes point r's 102
-// features into row r of the warpgroup's bf16 A operand; one thread issues the layer's tcgen05.mma
-// (kind::f16, bf16 x bf16 -> f32, M = 128 points, N = 64 neurons, K = 16 per instruction) against the
-// layer's weights; the accumulator lives in the warpgroup's 64 tensor-memory columns; tcgen05.commit
-// signals the warpgroup's mbarrier when the layer's MMAs are done.  Thread r then reads row r of the
-// accumulator (tcgen05.ld, 32 lanes x 32 columns per instruction), applies SiLU and writes the bf16
-// activations back as row r of the next layer's A operand.  The output layer (64 -> 1) is one more
-// MMA (N = 16, weights in column 0), read back as one tensor-memory column, plus the fp32 bias.  Each
-// thread loads its point of the warpgroup's next tile while the current tile's layers run.
-// Warpgroups synchronise on their own named barriers (ids 1..TC_NWG).
+// arithmetic overlaps the other warpgroups' MMAs.  Both operands a warpgroup produces live in its
+// 128 tensor-memory columns: the fp32 accumulator D (columns 0-63) and the bf16 A operand (columns
+// 64-119, two bf16 per column, row r in lane r), so shared memory carries only the weights (the B
+// operands).  In a warpgroup, thread r computes point r's 102 features and stores them as row r of A
+// (tcgen05.st); one thread issues the layer's tcgen05.mma (kind::f16, A from tensor memory, B from
+// shared memory, bf16 x bf16 -> f32, M = 128 points, N = 64 neurons, K = 16 per instruction);
+// tcgen05.commit signals the warpgroup's mbarrier when the layer's MMAs are done.  Thread r then reads
+// row r of D (tcgen05.ld), applies SiLU and stores the bf16 activations as row r of the next layer's A.
+// The output layer (64 -> 1) is one more MMA (N = 16, weights in column 0), read back as one column,
+// plus the fp32 bias.  Each thread loads its point of the warpgroup's next tile while the current
+// tile's layers run.  Warpgroups synchronise on their own named barriers (ids 1..TC_NWG).
 //
-// Operand layout: K-major, no swizzle, 8-row x 16-byte core matrices; the core matrix of row group
-// R and column group C of a matrix with K columns starts at byte (R * K / 8 + C) * 128, so the
-// descriptor of a 16-column step has a leading-dimension offset (between the two column groups) of
+// Weight layout (B, shared memory): K-major, no swizzle, 8-row x 16-byte core matrices; the core matrix
+// of row group R and column group C of a matrix with K columns starts at byte (R * K / 8 + C) * 128, so
+// the descriptor of a 16-column step has a leading-dimension offset (between the two column groups) of
 // 128 bytes and a stride offset (between row groups) of K * 16 bytes.
 //
 // Numerics are those of the mma.sync path: weights and activations in bf16, fp32 accumulation,
@@ -36,11 +37,13 @@ namespace {
 constexpr int TC_M = 128;                  // points per tile
 // layer 1 (K = TC_K1): 102 features, ones in columns 102 (bias high part) and 103 (remainder);
 // layers 2-4 (K = TC_KH): 64 activations, ones in columns 64 and 65
-constexpr int TC_COLS = 64;                // tensor-memory columns of one accumulator (N = 64, fp32)
-// tensor-memory columns a block allocates: a power of two >= 32 covering every warpgroup's accumulator
+constexpr int TC_COLS = 128;               // tensor-memory columns of a warpgroup: D at 0 (64), A at TC_ACOL
+constexpr int TC_ACOL = 64;                // A: TC_K1 / 2 = 56 columns (layer 1), TC_KH / 2 = 40 (the others)
+static_assert(TC_ACOL + TC_K1 / 2 <= TC_COLS, "the A operand does not fit beside the accumulator");
+// tensor-memory columns a block allocates: a power of two >= 32 covering every warpgroup's columns
 constexpr int TC_TMEM_COLS = TC_NWG * TC_COLS <= 32 ? 32 : TC_NWG * TC_COLS <= 64 ? 64 : TC_NWG * TC_COLS <= 128 ? 128
                              : TC_NWG * TC_COLS <= 256 ? 256 : 512;
-static_assert(TC_NWG * TC_COLS <= 512, "the warpgroups' accumulators exceed the tensor memory of an SM");
+static_assert(TC_NWG * TC_COLS <= 512, "the warpgroups' columns exceed the tensor memory of an SM");
 // instruction descriptor of kind::f16 with bf16 A and B (K-major, no negation) and an f32 D, for N columns
 constexpr uint32_t tc_idesc(int n) {
     return (1u << 4)                          // D format f32
@@ -76,11 +79,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
-__device__ __forceinline__ void tc_mma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+// A from tensor memory (taddr), B from shared memory (descriptor)
+__device__ __forceinline__ void tc_mma_ts(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "r"(atmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
@@ -100,6 +105,21 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&v)[32]) {
 __device__ __forceinline__ void tc_ld1(uint32_t taddr, uint32_t& v) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(v) : "r"(taddr) : "memory");
 }
+// this warp's 32 lanes, N consecutive columns from taddr (thread i: lane i)
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr), "r"(v[0]),
+                 "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t* v) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // named barrier of the warpgroup (id 1 + wg; id 0 is __syncthreads)
@@ -115,9 +135,6 @@ __device__ __forceinline__ bool wg_sync_or(int wg, bool p) {
     return r != 0;
 }
 
-__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
-}
 
 // SiLU of a pair of accumulator words holding h = z / 2: h + h tanh(h), as a bf16 pair.
 __device__ __forceinline__ uint32_t silu_half2(uint32_t x, uint32_t y) {
@@ -236,11 +253,10 @@ __global__ void __launch_bounds__(TC_M * TC_NWG, 1) k_nsdf_mlp_tc(TcArgs a) {
     extern __shared__ __align__(128) uint8_t smem_tc[];
     uint8_t* sW = smem_tc;
     const int wg = threadIdx.x >> 7, tid = threadIdx.x & (TC_M - 1), warp = tid >> 5;   // warpgroup, row, warp in it
-    uint8_t* sA = smem_tc + TC_WBYTES + (size_t)wg * TC_ABYTES;
-    const uint32_t uW = smem_u32(sW), uA = smem_u32(sA);
-    const uint32_t bars = smem_u32(smem_tc + TC_WBYTES + (size_t)TC_NWG * TC_ABYTES);
+    const uint32_t uW = smem_u32(sW);
+    const uint32_t bars = smem_u32(smem_tc + TC_WBYTES);
     const uint32_t bar = bars + 8u * wg;
-    uint32_t* slot = reinterpret_cast<uint32_t*>(smem_tc + TC_WBYTES + (size_t)TC_NWG * TC_ABYTES + 8 * TC_NWG);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(smem_tc + TC_WBYTES + 8 * TC_NWG);
 
     for (int i = threadIdx.x; i < TC_WBYTES / 16; i += blockDim.x)
         reinterpret_cast<uint4*>(sW)[i] = reinterpret_cast<const uint4*>(a.wtc)[i];
@@ -256,8 +272,9 @@ __global__ void __launch_bounds__(TC_M * TC_NWG, 1) k_nsdf_mlp_tc(TcArgs a) {
     __syncthreads();
     tc_fence_after();
     const float b5 = reinterpret_cast<const float*>(sW + TC_OFF_B5)[0];   // staged above
-    const uint32_t tmem = *slot + (uint32_t)(wg * TC_COLS);           // this warpgroup's accumulator
-    const uint32_t myLanes = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 accumulator rows
+    const uint32_t tD = *slot + (uint32_t)(wg * TC_COLS);             // this warpgroup's accumulator
+    const uint32_t tA = tD + TC_ACOL;                                 // and its A operand
+    const uint32_t lanes = (uint32_t)(warp * 32) << 16;               // this warp's 32 rows
     const Frame fr = a.fr;
     const long long total = MODE == TC_CLASSIFY ? a.vtot : (long long)a.count;
     const float limit = a.margin / fr.cell + a.slackCells;
@@ -275,40 +292,39 @@ __global__ void __launch_bounds__(TC_M * TC_NWG, 1) k_nsdf_mlp_tc(TcArgs a) {
         tc_fence_after();
         return true;
     };
-    // one layer: K/16 MMAs of the A buffer (row stride kt columns) against weights at byte offset wOff
+    // one layer: K/16 MMAs of A (tensor memory, 8 columns per step) against weights at byte offset wOff
     auto issue = [&](int kt, int wOff, uint32_t idesc) {
         if (tid == 0) {
             tc_fence_after();
             const uint32_t sbo = (uint32_t)kt * 16u;
             for (int j = 0; j < kt / 16; ++j)
-                tc_mma(tmem, smem_desc(uA + 256u * j, 128u, sbo), smem_desc(uW + wOff + 256u * j, 128u, sbo), idesc,
-                       j > 0);
+                tc_mma_ts(tD, tA + 8u * j, smem_desc(uW + wOff + 256u * j, 128u, sbo), idesc, j > 0);
             tc_commit(bar);
         }
     };
-    // row `tid` of the accumulator through SiLU into row `tid` of the next A operand (K = TC_KH)
-    auto hidden_epilogue = [&](bool writeOnes) {
-        uint32_t v[32], u[32];
-        tc_ld32(myLanes + 0, v);
-        tc_ld32(myLanes + 32, u);
-        tc_wait_ld();
-#pragma unroll
-        for (int c = 0; c < 4; ++c)
-            st_shared_v4(uA + kmajor_off(tid, 8 * c, TC_KH), silu_half2(v[8 * c], v[8 * c + 1]),
-                         silu_half2(v[8 * c + 2], v[8 * c + 3]), silu_half2(v[8 * c + 4], v[8 * c + 5]),
-                         silu_half2(v[8 * c + 6], v[8 * c + 7]));
-#pragma unroll
-        for (int c = 0; c < 4; ++c)
-            st_shared_v4(uA + kmajor_off(tid, 32 + 8 * c, TC_KH), silu_half2(u[8 * c], u[8 * c + 1]),
-                         silu_half2(u[8 * c + 2], u[8 * c + 3]), silu_half2(u[8 * c + 4], u[8 * c + 5]),
-                         silu_half2(u[8 * c + 6], u[8 * c + 7]));
-        if (writeOnes) {
-            st_shared_v4(uA + kmajor_off(tid, HID, TC_KH), BF16_ONES, 0u, 0u, 0u);
-            st_shared_v4(uA + kmajor_off(tid, HID + 8, TC_KH), 0u, 0u, 0u, 0u);
-        }
-        fence_proxy_async_smem();
+    // A written by every thread of the warpgroup: make it visible to the MMA issued after the barrier
+    auto publish_a = [&]() {
+        tc_wait_st();
         tc_fence_before();
         wg_sync(wg);
+    };
+    // row `tid` of the accumulator through SiLU into row `tid` of the next A (K = TC_KH: 64 activations,
+    // then the bias columns of ones and zeros)
+    auto hidden_epilogue = [&]() {
+        uint32_t v[32], u[32];
+        tc_ld32(tD + lanes + 0, v);
+        tc_ld32(tD + lanes + 32, u);
+        tc_wait_ld();
+        uint32_t h[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) h[c] = silu_half2(v[2 * c], v[2 * c + 1]);
+        tc_st16(tA + lanes + 0, h);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) h[c] = silu_half2(u[2 * c], u[2 * c + 1]);
+        tc_st16(tA + lanes + 16, h);
+        const uint32_t ones[8] = {BF16_ONES, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        tc_st8(tA + lanes + 32, ones);
+        publish_a();
     };
 
     // this thread's point of a tile (the query pose for points, the sample's own pose for samples)
@@ -336,33 +352,33 @@ __global__ void __launch_bounds__(TC_M * TC_NWG, 1) k_nsdf_mlp_tc(TcArgs a) {
             uint32_t w[56];
             point_features((px - fr.cx) * fr.ihx, (py - fr.cy) * fr.ihy, (pz - fr.cz) * fr.ihz, a0 * fr.poseScale,
                            a1 * fr.poseScale, a2 * fr.poseScale, valid, w);
-#pragma unroll
-            for (int c = 0; c < TC_K1 / 8; ++c)
-                st_shared_v4(uA + kmajor_off(tid, 8 * c, TC_K1), w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+            tc_st16(tA + lanes + 0, w);
+            tc_st16(tA + lanes + 16, w + 16);
+            tc_st16(tA + lanes + 32, w + 32);
+            tc_st8(tA + lanes + 48, w + 48);
         }
-        fence_proxy_async_smem();
-        wg_sync(wg);
+        publish_a();
 
         issue(TC_K1, TC_OFF_W1, TC_IDESC);
         if (!layer_done()) break;
-        hidden_epilogue(true);
+        hidden_epilogue();
         issue(TC_KH, TC_OFF_W2, TC_IDESC);
         if (!layer_done()) break;
-        hidden_epilogue(false);
+        hidden_epilogue();
         issue(TC_KH, TC_OFF_W3, TC_IDESC);
         if (!layer_done()) break;
-        hidden_epilogue(false);
+        hidden_epilogue();
         issue(TC_KH, TC_OFF_W4, TC_IDESC);
         if (!layer_done()) break;
-        hidden_epilogue(false);
+        hidden_epilogue();
         // output layer: y = b5 + sum_k w5[k] SiLU(z4)[k] (the ones columns meet zero weights)
         issue(TC_KH, TC_OFF_W5, TC_IDESC5);
         if (!layer_done()) break;
         uint32_t acc;
-        tc_ld1(myLanes, acc);
+        tc_ld1(tD + lanes, acc);
         tc_wait_ld();
         const float y = b5 + __uint_as_float(acc);
-        tc_fence_before();   // the next tile's MMAs overwrite the accumulator after the warpgroup's next barrier
+        tc_fence_before();   // the next tile's stores and MMAs reuse the columns after the warpgroup's next barrier
 
         if (valid) {
             if constexpr (MODE == TC_CLASSIFY) {
@@ -395,8 +411,8 @@ static cudaError_t launch_tc(const TcArgs& a, long long total, cudaStream_t s) {
     if (total <= 0) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_nsdf_mlp_tc<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
     if (e != cudaSuccess) return e;
-    // resident blocks per SM: shared memory (each block holds the weights and one operand per
-    // warpgroup) and tensor memory (512 columns per SM) decide it
+    // resident blocks per SM: tensor memory (512 columns per SM) and shared memory (the weights)
+    // decide it
     int dev = 0, smemPerSM = 0;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smemPerSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
