@@ -351,6 +351,11 @@ int tfx_batch_destroy(tfx_batch batch);
 int tfx_batch_add_sdf(tfx_batch batch, tfx_sdf sdf, tfx_mesh mesh, int nx, int ny, int nz, int* index);
 /* Registers a hair object that collides with SDF `sdf_index` (-1: no collision). */
 int tfx_batch_add_hair(tfx_batch batch, tfx_hair hair, int sdf_index, int* index);
+/* Makes hair object `hair_index` also collide with SDF `sdf_index`, after the SDFs it already collides
+ * with, in the order of these calls: Simulation::RunCollision applies every collision mesh to every
+ * hair object in turn (src/Simulation.cpp:106-118).  The hair object must have been added with an
+ * SDF, and collides with each SDF once. */
+int tfx_batch_add_hair_collision(tfx_batch batch, int hair_index, int sdf_index);
 /* Builds the object / work / tile tables and captures the frame graphs (reserved must be 0). */
 int tfx_batch_build(tfx_batch batch, int reserved);
 /* Times the candidate launch shapes over `frames` frames each on the current inputs, restores every
@@ -423,7 +428,9 @@ int tfx_batch_synchronize(tfx_batch batch);
 int tfx_batch_describe(tfx_batch batch, char* buf, size_t len, int32_t* launches_per_frame);
 /* Runs one frame like tfx_batch_run but with direct launches and CUDA events between its parts;
  * waits for it and returns the milliseconds of each part: [0] = mesh skinning + SDF rebuild,
- * [1..] = the fused strand launch of each vertices-per-strand class present (ascending n). */
+ * [1..] = the fused strand launch of each vertices-per-strand class present (ascending n), then the
+ * follow/collide launch of each class, then (when some hair object collides with further SDFs,
+ * tfx_batch_add_hair_collision) those collisions. */
 int tfx_batch_profile_frame(tfx_batch batch, float* part_ms, int max_parts, int* num_parts);
 
 /* ---------------------------------------------------------------------------------- learned collision proxy */

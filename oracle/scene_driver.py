@@ -59,6 +59,7 @@ class OraclePipeline:
         self.hair = [OracleHair(o.asset, dtype) for o in scene.objects]
         self.consts = [OracleConstants(o.asset.verts_per_strand, o.asset.follow_per_guide) for o in scene.objects]
         self.sdf_words = [None] * len(scene.objects)
+        self.more_words = [[None] * len(o.more) for o in scene.objects]   # further colliders
         self.frame = 0
         self.stage_seconds: dict[str, float] = {}
 
@@ -79,6 +80,10 @@ class OraclePipeline:
                 t = self._t("BoneSkinning", t)
                 self.sdf_words[i] = sdf_build(fin.grids[i], skinned, o.mesh.indices, self.dtype, self.threads)
                 t = self._t("SDFBuild", t)
+            for k, c in enumerate(o.more):
+                skinned = mesh_skin(c.mesh.vertices, c.mesh.skinning, fin.more_bones[i][k], self.threads)
+                self.more_words[i][k] = sdf_build(fin.more_grids[i][k], skinned, c.mesh.indices, self.dtype, self.threads)
+                t = self._t("SDFBuild", t)
         order = [(STAGE_INTEGRATE, "IntegrationAndGlobalShapeConstraints"), (STAGE_STRAND_LEVEL, "CalculateStrandLevelData"),
                  (STAGE_VSP, "VelocityShockPropagation"), (STAGE_LOCAL_SHAPE, "LocalShapeConstraints"),
                  (STAGE_LENGTH_WIND, "LengthConstriantsWindAndCollision"), (STAGE_FOLLOW, "UpdateFollowHairVertices")]
@@ -94,5 +99,8 @@ class OraclePipeline:
             if o.mesh is not None:
                 g = fin.grids[i]
                 sdf_collide(g, self.sdf_words[i], self._margin_world(o, g), h, self.threads)
+            for k, c in enumerate(o.more):   # Simulation::RunCollision: every collision mesh, in order
+                g = fin.more_grids[i][k]
+                sdf_collide(g, self.more_words[i][k], self._margin_world(c, g), h, self.threads)
         self._t("CollideHairVerticesWithSdf", t)
         self.frame += 1

@@ -15,6 +15,9 @@ the frame-parity tests that run where the reference tree is absent.
   (oracle/mesh_ref), then the triangles with a corner within 4 cm of a vertex of the hair slice,
   re-indexed.  Follow bone: the sample's frenchHornMonster_root_JNT
   (src/TressFXSample.cpp:473-480).
+* Hands: Ratboy_left_hand.tfxmesh and Ratboy_right_hand.tfxmesh whole (renamed bones as above), the
+  sample's two further collision meshes (follow bones frenchHornMonster_L/R_LowerArm_JNT, 32 cells
+  across, margin 0.5: src/TressFXSample.cpp:481-500).
 
 The raw slice (guide positions, bone records, bone names) is kept too, so that a test can write the
 same files again and check the library's own loader against the reference's output.
@@ -42,6 +45,8 @@ GUIDES = 120
 FOLLOW, TIP, RADIUS, SEED = 2, 2.0, 0.012, 11
 BODY_RADIUS = 0.04
 FOLLOW_BONE = b"frenchHornMonster_root_JNT"
+HANDS = (("left_hand", "Ratboy_left_hand.tfxmesh", b"frenchHornMonster_L_LowerArm_JNT"),
+         ("right_hand", "Ratboy_right_hand.tfxmesh", b"frenchHornMonster_R_LowerArm_JNT"))
 
 
 def mesh_bone_names(text: str) -> list[bytes]:
@@ -84,9 +89,13 @@ def main() -> None:
     body_text = (REAL_ASSET_DIR / "Ratboy_body.tfxmesh").read_text()
     body_names = mesh_bone_names(body_text)
 
+    hand_texts = [(REAL_ASSET_DIR / f).read_text() for _, f, _ in HANDS]
     ids: dict[bytes, int] = {}
     for n in body_names + [h.rstrip(b"\0") for h in hair_names]:
         ids.setdefault(n, len(ids))
+    for t in hand_texts:            # after the hair's and the body's, so their ids do not move
+        for n in mesh_bone_names(t):
+            ids.setdefault(n, len(ids))
     renamed_hair = [f"b{ids[h.rstrip(b'\0')]}".encode() + b"\0" for h in hair_names]
 
     rows = np.round(np.linspace(0, len(all_guides) - 1, GUIDES)).astype(np.int64)
@@ -106,6 +115,16 @@ def main() -> None:
         subprocess.run([str(mexe), str(d / "body.tfxmesh"), follow, str(d / "body.bin")], check=True,
                        capture_output=True)
         mcounts, mesh = read_mesh_dump(d / "body.bin")
+        hands = {}
+        for (name, _, bone), text in zip(HANDS, hand_texts):
+            (d / f"{name}.tfxmesh").write_text(rename_mesh_bones(text, ids))
+            subprocess.run([str(mexe), str(d / f"{name}.tfxmesh"), f"b{ids[bone]}", str(d / f"{name}.bin")], check=True,
+                           capture_output=True)
+            hc, hm = read_mesh_dump(d / f"{name}.bin")
+            hands[f"{name}_counts"] = hc
+            hands[f"{name}_vertices"] = hm["bind_pose"].reshape(-1, 8)
+            hands[f"{name}_indices"] = hm["indices"]
+            hands[f"{name}_skinning"] = hm["skinning"].reshape(-1, 8)
 
     from scipy.spatial import cKDTree
     pos = arrays["positions"].reshape(-1, 4)[:, :3].astype(np.float64)
@@ -118,10 +137,14 @@ def main() -> None:
     remap[used] = np.arange(len(used))
     sub_tri = remap[tri[keep]].astype(np.uint32)
 
+    # the reference's loader never writes the tangents' w (its value is whatever the allocation held);
+    # the fixture takes 0 there, as the library's loader writes
+    tangents = arrays["tangents"].reshape(-1, 4).copy()
+    tangents[:, 3] = 0.0
     out = dict(
         guide_rows=rows.astype(np.int32), raw_guides=guides, raw_bones=bones.astype(np.int32),
         raw_weights=weights.astype(np.float32), raw_bone_names=np.array(renamed_hair, dtype=object).astype(bytes),
-        counts=counts, positions=arrays["positions"], tangents=arrays["tangents"],
+        counts=counts, positions=arrays["positions"], tangents=tangents.reshape(-1),
         follow_root_offsets=arrays["follow_root_offsets"], rest_lengths=arrays["rest_lengths"],
         bone_skinning=arrays["bone_skinning"],
         mesh_counts=mcounts, mesh_triangle_rows=keep.astype(np.int32), mesh_vertices=verts[used].copy(),
@@ -129,8 +152,10 @@ def main() -> None:
         num_bones=np.int32(len(ids)), follow_bone=np.int32(ids[FOLLOW_BONE]),
         options=np.array([FOLLOW, TIP, RADIUS, SEED], np.float64),
         loader_digests=np.array(json.dumps(digests(counts, arrays), sort_keys=True)),
+        **hands,
     )
     np.savez_compressed(HERE / "ratboy_subset.npz", **out)
+    print(f"hands {[int(hands[f'{n}_counts'][1]) for n, _, _ in HANDS]} triangles")
     print(f"hair {counts.tolist()}, body {len(keep)} of {len(tri)} triangles, {len(used)} vertices, "
           f"{len(ids)} bones, file {(HERE / 'ratboy_subset.npz').stat().st_size} bytes")
 

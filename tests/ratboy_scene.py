@@ -13,10 +13,11 @@ from pathlib import Path
 
 import numpy as np
 
-from tressfx_gb300.synthetic import HairAsset, Mesh, Scene, SceneObject, _settings, bone_matrix, rot_x, rot_y
+from tressfx_gb300.synthetic import Collider, HairAsset, Mesh, Scene, SceneObject, _settings, bone_matrix, rot_x, rot_y
 
 FIXTURE = Path(__file__).resolve().parent / "golden" / "ratboy_subset.npz"
 SDF_CELLS_X = 50          # TressFXCollisionMeshDescription of the body (src/TressFXSample.cpp:473-480)
+HAND_CELLS_X, HAND_MARGIN = 32, 0.5   # and of each hand (:481-500)
 PIVOT = np.array([0.0, 0.55, 0.05])
 
 
@@ -49,7 +50,19 @@ def bones_fn(num_bones: int, amplitude_deg: float = 25.0, hz: float = 1.0):
     return fn
 
 
-def scene(frames: int = 12, margin_cells: float = 0.5) -> Scene:
+def grid_by_reference_rule(mesh: Mesh, cells_x: int):
+    """(dims, cell, centre) as TressFXSDFCollision sizes a grid (TressFXSDFCollision.cpp:43-68)."""
+    p = mesh.vertices[:, :3].astype(np.float32)
+    lo, hi = p.min(0), p.max(0)
+    cell = np.float32((hi[0] - lo[0]) / np.float32(cells_x))
+    pad = np.float32(int(0.8 * cells_x)) * cell
+    dims = tuple(int((hi[i] - lo[i] + 2 * pad) / cell) for i in range(3))
+    return dims, float(cell), ((lo + hi) / 2).astype(np.float64)
+
+
+def scene(frames: int = 12, margin_cells: float = 0.5, hands: bool = False) -> Scene:
+    """The slice colliding with the body; with `hands`, then with each hand too, as the sample collides
+    the mohawk with all three meshes (src/Simulation.cpp:106-118)."""
     f = load()
     asset = hair_asset(f)
     mesh = Mesh(vertices=f["mesh_vertices"].astype(np.float32).copy(), indices=f["mesh_indices"].astype(np.uint32).copy(),
@@ -57,14 +70,19 @@ def scene(frames: int = 12, margin_cells: float = 0.5) -> Scene:
     st = _settings(vsp_coeff=0.758, vsp_accel_threshold=1.208, local_constraint_stiffness=0.908,
                    local_constraints_iterations=3, global_constraint_stiffness=0.408, global_constraints_range=0.308,
                    length_constraints_iterations=3, damping=0.068, gravity_magnitude=0.09)
-    p = mesh.vertices[:, :3].astype(np.float32)
-    lo, hi = p.min(0), p.max(0)
-    cell = np.float32((hi[0] - lo[0]) / np.float32(SDF_CELLS_X))
-    pad = np.float32(int(0.8 * SDF_CELLS_X)) * cell
-    dims = tuple(int((hi[i] - lo[i] + 2 * pad) / cell) for i in range(3))
+    dims, cell, centre = grid_by_reference_rule(mesh, SDF_CELLS_X)
     nb = int(f["num_bones"])
     fn = bones_fn(nb)
-    obj = SceneObject(asset, st, fn, mesh, fn, dims, float(cell), ((lo + hi) / 2).astype(np.float64),
-                      follow_bone=int(f["follow_bone"]), collision_margin_cells=margin_cells)
-    return Scene(f"ratboy_slice_{asset.num_guide_strands}x{asset.verts_per_strand}_F{asset.follow_per_guide}",
-                 [obj], frames=frames)
+    obj = SceneObject(asset, st, fn, mesh, fn, dims, cell, centre, follow_bone=int(f["follow_bone"]),
+                      collision_margin_cells=margin_cells)
+    name = f"ratboy_slice_{asset.num_guide_strands}x{asset.verts_per_strand}_F{asset.follow_per_guide}"
+    if hands:
+        for side in ("left_hand", "right_hand"):
+            hm = Mesh(vertices=f[f"{side}_vertices"].astype(np.float32).copy(),
+                      indices=f[f"{side}_indices"].astype(np.uint32).copy(),
+                      skinning=f[f"{side}_skinning"].astype(np.float32).copy())
+            hd, hc, hctr = grid_by_reference_rule(hm, HAND_CELLS_X)
+            obj.more.append(Collider(hm, fn, hd, hc, hctr, follow_bone=int(f[f"{side}_counts"][2]),
+                                     collision_margin_cells=HAND_MARGIN))
+        name += "_body_hands"
+    return Scene(name, [obj], frames=frames)

@@ -30,9 +30,9 @@ def _compare(gpu, ora, what):
 
 
 def _contacts(sc) -> int:
-    """Vertices whose final position the body changed (oracle with and without the mesh)."""
+    """Vertices whose final position the collision meshes changed (oracle with and without them)."""
     o = sc.objects[0]
-    bare = dataclasses.replace(sc, objects=[dataclasses.replace(o, mesh=None, mesh_bone_fn=None)])
+    bare = dataclasses.replace(sc, objects=[dataclasses.replace(o, mesh=None, mesh_bone_fn=None, more=[])])
     a, b = OraclePipeline(sc), OraclePipeline(bare)
     for f in range(FRAMES):
         a.step(FrameInputs(sc, f))
@@ -40,10 +40,13 @@ def _contacts(sc) -> int:
     return int((a.hair[0].pos != b.hair[0].pos).any(axis=1).sum())
 
 
-@pytest.mark.parametrize("margin", [0.0, 0.5])
+@pytest.mark.parametrize("margin,hands", [(0.0, False), (0.5, False), (0.0, True)],
+                         ids=["body", "body_margin_half_cell", "body_and_hands"])
 @pytest.mark.parametrize("path", ["plain", "batched"])
-def test_ratboy_slice_frames(ctx, path, margin):
-    sc = ratboy_scene.scene(FRAMES, margin_cells=margin)
+def test_ratboy_slice_frames(ctx, path, margin, hands):
+    """With `hands`, the sample's set-up: the mohawk collides with the body (margin 0), then with each
+    hand (32 cells across, margin 0.5), each on its own SDF."""
+    sc = ratboy_scene.scene(FRAMES, margin_cells=margin, hands=hands)
     assert _contacts(sc) > 100
     gpu = PlainPipeline(ctx, sc) if path == "plain" else BatchedPipeline(ctx, sc, autotune_frames=0)
     ora = OraclePipeline(sc)

@@ -212,6 +212,7 @@ _PROTOS = {
     "tfx_batch_destroy": (C.c_int, [P]),
     "tfx_batch_add_sdf": (C.c_int, [P, P, P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "tfx_batch_add_hair": (C.c_int, [P, P, C.c_int, C.POINTER(C.c_int)]),
+    "tfx_batch_add_hair_collision": (C.c_int, [P, C.c_int, C.c_int]),
     "tfx_batch_build": (C.c_int, [P, C.c_int]),
     "tfx_batch_set_option": (C.c_int, [P, C.c_int, C.c_int]),
     "tfx_batch_get_option": (C.c_int, [P, C.c_int, C.POINTER(C.c_int)]),

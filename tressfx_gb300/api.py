@@ -408,6 +408,11 @@ class Batch:
         self._keep.append(hair)
         return i.value
 
+    def add_hair_collision(self, hair_index: int, sdf_index: int) -> None:
+        """Hair object `hair_index` also collides with SDF `sdf_index`, after its earlier SDFs."""
+        check(A.lib().tfx_batch_add_hair_collision(self.handle, int(hair_index), int(sdf_index)),
+              "tfx_batch_add_hair_collision")
+
     def build(self) -> None:
         check(A.lib().tfx_batch_build(self.handle, 0), "tfx_batch_build")
 

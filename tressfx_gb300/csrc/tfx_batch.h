@@ -23,6 +23,14 @@ struct BatchObject {
     const SdfFrame* sdfFrame;      // this frame's grid + margin (inside the device frame block)
 };
 
+// One (hair object, SDF) pair of a collision level: level k holds every object's k-th SDF after its
+// first (tfx_batch_add_hair_collision), so a level's pairs touch distinct objects and run in one launch.
+struct BatchCollide {
+    int obj;                  // index into the object table
+    int sdf;                  // index into the SDF table
+    long long firstVertex;    // prefix over the level's pairs of their objects' vertices
+};
+
 // A group of guide strands of one object (at most fused_group_size(n)): one block of the fused
 // kernel at a time.
 struct WorkItem {
@@ -119,6 +127,9 @@ cudaError_t launch_fused_strands(const FusedLaunch& fl, cudaStream_t s);
 // k_local_sweep over the groups of fl (mode 1 has run on them, mode 2 runs after)
 cudaError_t launch_local_sweep(const FusedLaunch& fl, cudaStream_t s);
 cudaError_t launch_follow_collide(const FollowLaunch& fl, cudaStream_t s);
+// CollideHairVerticesWithSdf_forward of one collision level's pairs
+cudaError_t launch_collide_level(const BatchObject* objs, const BatchSdf* sdfs, const BatchCollide* pairs, int npairs,
+                                 long long totalVertices, cudaStream_t s);
 cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s);
 cudaError_t launch_batch_sdf(const SdfBatchLaunch& l, cudaStream_t s);
 // Every object's positions, consecutively (first[i] = object i's first vertex), into `out` as float4 or packed xyz.

@@ -48,6 +48,10 @@ struct tfx_batch_t {
     tfx_context ctx = nullptr;
     std::vector<tfx_hair> hairs;
     std::vector<int> hairSdf;
+    std::vector<std::vector<int>> hairMoreSdf;   // per hair object: further SDFs, in collision order
+    std::vector<BatchCollide*> levelPairs;       // per collision level: its pairs on the device
+    std::vector<int> levelCount;
+    std::vector<long long> levelVertices;
     std::vector<bool> hairSet;
     std::vector<tfx_sdf> sdfs;
     std::vector<tfx_mesh> sdfMesh;
@@ -155,6 +159,8 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
     if (b->devArena) cudaFree(b->devArena);
     if (b->expandedArena) cudaFree(b->expandedArena);
     if (b->tileArena) cudaFree(b->tileArena);
+    for (auto t : b->levelPairs)
+        if (t) cudaFree(t);
     for (auto& c : b->classes)
         if (c.items) cudaFree(c.items);
     for (auto h : b->hairs) context_release(h->ctx);
@@ -198,8 +204,29 @@ extern "C" int tfx_batch_add_hair(tfx_batch b, tfx_hair hair, int sdf_index, int
     context_retain(hair->ctx);
     b->hairs.push_back(hair);
     b->hairSdf.push_back(sdf_index);
+    b->hairMoreSdf.emplace_back();
     b->hairSet.push_back(false);
     if (index) *index = (int)b->hairs.size() - 1;
+    return TFX_OK;
+}
+
+extern "C" int tfx_batch_add_hair_collision(tfx_batch b, int hair_index, int sdf_index) {
+    if (!b) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair_collision: null batch");
+    if (b->built) return batch_fail_built("tfx_batch_add_hair_collision");
+    if (hair_index < 0 || hair_index >= (int)b->hairs.size())
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair_collision: hair index %d of %zu", hair_index,
+                    b->hairs.size());
+    if (sdf_index < 0 || sdf_index >= (int)b->sdfs.size())
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair_collision: SDF index %d of %zu", sdf_index,
+                    b->sdfs.size());
+    if (b->hairSdf[hair_index] < 0)
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair_collision: hair object %d was added without an SDF",
+                    hair_index);
+    auto& more = b->hairMoreSdf[hair_index];
+    if (sdf_index == b->hairSdf[hair_index] || std::find(more.begin(), more.end(), sdf_index) != more.end())
+        return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_add_hair_collision: hair object %d already collides with SDF %d",
+                    hair_index, sdf_index);
+    more.push_back(sdf_index);
     return TFX_OK;
 }
 
@@ -296,6 +323,16 @@ static int launch_follows(tfx_batch b, BatchClass& c, cudaStream_t s) {
     return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: follow/collide launch");
 }
 
+// The objects' further SDFs, level by level, after every follow/collide launch.
+static int launch_collide_levels(tfx_batch b, cudaStream_t s) {
+    for (size_t k = 0; k < b->levelPairs.size(); ++k) {
+        cudaError_t e = launch_collide_level(b->objTable, b->sdfTable, b->levelPairs[k], b->levelCount[k],
+                                             b->levelVertices[k], s);
+        if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: collision level launch");
+    }
+    return TFX_OK;
+}
+
 // One frame as direct launches, in dependency order on one stream, with an event after each part:
 // part 0 = mesh skinning + SDF build, then one part per class for k_fused_strands, then one per
 // class for k_follow_collide (used by profiling).
@@ -319,6 +356,10 @@ static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* 
     for (auto& c : b->classes) {
         if (c.numItems == 0) continue;
         if (int r = launch_follows(b, c, s)) return r;
+        mark();
+    }
+    if (!b->levelPairs.empty()) {
+        if (int r = launch_collide_levels(b, s)) return r;
         mark();
     }
     if (partMs) {
@@ -359,7 +400,7 @@ static int launch_frame_forked(tfx_batch b, cudaStream_t s) {
     for (auto& c : b->classes)
         if (c.numItems > 0)
             if (int r = launch_follows(b, c, s)) return r;
-    return TFX_OK;
+    return launch_collide_levels(b, s);
 }
 
 static int capture_graphs(tfx_batch b) {
@@ -390,6 +431,7 @@ static int capture_graphs(tfx_batch b) {
     }
     int launches = (b->totalMeshVerts > 0 ? 1 : 0) + sdfLaunches;
     for (auto& c : b->classes) launches += c.numItems > 0 ? (c.splitSweeps ? 4 : 2) : 0;
+    for (size_t k = 0; k < b->levelPairs.size(); ++k) launches += b->levelVertices[k] > 0 ? 1 : 0;
     b->launchesPerFrame = launches;
     return TFX_OK;
 }
@@ -666,6 +708,27 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
         objs[o].sdf8 = nullptr;   // set by apply_expand_mode
     }
     TFX_CUDA(cudaMemcpy(b->objTable, objs.data(), sizeof(BatchObject) * nobj, cudaMemcpyHostToDevice), "tfx_batch: objects");
+
+    // collision levels: level k = every object's k-th further SDF (distinct objects, one launch each)
+    size_t levels = 0;
+    for (auto& m : b->hairMoreSdf) levels = std::max(levels, m.size());
+    for (size_t k = 0; k < levels; ++k) {
+        std::vector<BatchCollide> pairs;
+        long long first = 0;
+        for (int o = 0; o < nobj; ++o) {
+            if (b->hairMoreSdf[o].size() <= k) continue;
+            const HairView& v = b->hairs[o]->view;
+            pairs.push_back(BatchCollide{o, b->hairMoreSdf[o][k], first});
+            first += (long long)v.G * (v.F + 1) * v.n;
+        }
+        BatchCollide* d = nullptr;
+        TFX_CUDA(cudaMalloc(&d, sizeof(BatchCollide) * pairs.size()), "tfx_batch: collision levels");
+        b->levelPairs.push_back(d);
+        TFX_CUDA(cudaMemcpy(d, pairs.data(), sizeof(BatchCollide) * pairs.size(), cudaMemcpyHostToDevice),
+                 "tfx_batch: collision levels");
+        b->levelCount.push_back((int)pairs.size());
+        b->levelVertices.push_back(first);
+    }
 
     std::vector<BatchMesh> meshes;
     int firstVertex = 0;

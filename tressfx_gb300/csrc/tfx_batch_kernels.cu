@@ -30,6 +30,8 @@
 //  * k_follow_collide     - UpdateFollowHairVertices (TressFXSimulation.hlsl:978-1001) and the SDF
 //                           collision (TressFXSDFCollision.hlsl:531-595) of every guide and follow
 //                           vertex, after both.
+//  * k_collide_level      - the same collision with an object's further SDFs, one level (every object's
+//                           k-th further SDF) per launch, after k_follow_collide.
 // All per-vertex arithmetic is the reference's, in the same order, so every buffer matches the
 // plain path and the oracle bit for bit.
 #include "tfx_batch.h"
@@ -1128,6 +1130,44 @@ cudaError_t launch_follow_collide(const FollowLaunch& fl, cudaStream_t s) {
 cudaError_t launch_batch_mesh_skin(const BatchMesh* meshes, int nmeshes, int totalVerts, cudaStream_t s) {
     if (totalVerts <= 0) return cudaSuccess;
     k_batch_mesh_skin<<<(totalVerts + 255) / 256, 256, 0, s>>>(meshes, nmeshes, totalVerts);
+    return cudaGetLastError();
+}
+
+// CollideHairVerticesWithSdf_forward (TressFXSDFCollision.hlsl:531-595) of every vertex of a level's
+// objects against that pair's SDF (the decoded float grid), one thread per vertex; vertices 0 and 1 of a
+// strand are left alone, as the shader does.  Same arithmetic as k_sdf_collide.
+__global__ void __launch_bounds__(256) k_collide_level(const BatchObject* __restrict__ objs, const BatchSdf* __restrict__ sdfs,
+                                                       const BatchCollide* __restrict__ pairs, int npairs, long long total) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += stride) {
+        int lo = 0, hi = npairs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (pairs[mid].firstVertex <= i) lo = mid; else hi = mid - 1;
+        }
+        const BatchCollide pc = pairs[lo];
+        const HairView& h = objs[pc.obj].hair;
+        const long long v = i - pc.firstVertex;
+        const int local = (int)(v % h.n);
+        if (local == 0 || local == 1) continue;
+        const BatchSdf& sd = sdfs[pc.sdf];
+        const SdfGrid g = sd.frame->grid;
+        const float margin = sd.frame->margin;
+        const float* sdf = reinterpret_cast<const float*>(sd.words);
+        const float4 hv = h.pos[v];
+        float3 proj;
+        if (sdf_collide_point(sdf, g, margin, xyz(hv), proj)) {
+            h.pos[v] = with_xyz(hv, proj);
+            h.prev[v] = with_xyz(h.prev[v], proj);
+        }
+    }
+}
+
+cudaError_t launch_collide_level(const BatchObject* objs, const BatchSdf* sdfs, const BatchCollide* pairs, int npairs,
+                                 long long totalVertices, cudaStream_t s) {
+    if (npairs <= 0 || totalVertices <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)std::min<long long>((totalVertices + 255) / 256, (long long)sm_count() * 16);
+    k_collide_level<<<blocks, 256, 0, s>>>(objs, sdfs, pairs, npairs, totalVertices);
     return cudaGetLastError();
 }
 

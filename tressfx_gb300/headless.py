@@ -44,6 +44,8 @@ class FrameInputs:
         self.hair_bones = []
         self.mesh_bones = []
         self.grids = []
+        self.more_bones: list[list] = []   # per object: the bones and grids of its further colliders
+        self.more_grids: list[list] = []
         for o in scene.objects:
             st = dict(o.settings)
             st["wind_magnitude"] = wind_magnitude(scene, o, frame)
@@ -56,6 +58,9 @@ class FrameInputs:
             else:
                 self.mesh_bones.append(None)
                 self.grids.append(None)
+            mbs = [c.mesh_bone_fn(t) for c in o.more]
+            self.more_bones.append(mbs)
+            self.more_grids.append([sdf_grid_for(c, mb) for c, mb in zip(o.more, mbs)])
 
     @property
     def settings(self) -> list[A.SimSettings]:
@@ -86,6 +91,16 @@ class PlainPipeline:
             else:
                 self.meshes.append(None)
                 self.sdfs.append(None)
+        # further colliders: (mesh, sdf) per object, in collision order
+        self.more: list[list[tuple[CollisionMesh, SDFCollision]]] = []
+        for o in scene.objects:
+            pairs = []
+            for c in o.more:
+                m = CollisionMesh(ctx, c.mesh.vertices, c.mesh.indices, c.mesh.skinning)
+                s = SDFCollision(ctx, int(np.prod(c.sdf_dims)))
+                s.bind_mesh(m)
+                pairs.append((m, s))
+            self.more.append(pairs)
 
     def prepare(self, fin: FrameInputs) -> None:
         """Host side of a frame: UpdateSimulationParameters + UpdateBones for every object."""
@@ -99,10 +114,17 @@ class PlainPipeline:
             if m is not None:
                 m.skin(mb)
                 s.update(g)
+        for pairs, mbs, gs in zip(self.more, fin.more_bones, fin.more_grids):
+            for (m, s), mb, g in zip(pairs, mbs, gs):
+                m.skin(mb)
+                s.update(g)
         self.sim.simulate(self.hair)
-        for h, s, o, g in zip(self.hair, self.sdfs, self.scene.objects, fin.grids):
+        # Simulation::RunCollision: every collision mesh of an object, in order
+        for h, s, o, g, pairs, gs in zip(self.hair, self.sdfs, self.scene.objects, fin.grids, self.more, fin.more_grids):
             if s is not None:
                 s.collide(h, g, margin_world(o, g))
+            for (_, sm), c, gm in zip(pairs, o.more, gs):
+                sm.collide(h, gm, margin_world(c, gm))
         self.frame += 1
 
     def step(self, frame: int | None = None) -> FrameInputs:
@@ -112,7 +134,7 @@ class PlainPipeline:
         return fin
 
     def close(self) -> None:
-        for x in self.hair + self.meshes + self.sdfs:
+        for x in self.hair + self.meshes + self.sdfs + [x for pairs in self.more for pair in pairs for x in pair]:
             if x is not None:
                 x.close()
 
@@ -127,8 +149,13 @@ class BatchedPipeline(PlainPipeline):
         self.sdf_index: list[int] = []
         for m, s, o in zip(self.meshes, self.sdfs, scene.objects):
             self.sdf_index.append(self.batch.add_sdf(s, m, o.sdf_dims) if s is not None else -1)
-        for h, si in zip(self.hair, self.sdf_index):
+        self.more_index: list[list[int]] = []
+        for pairs, o in zip(self.more, scene.objects):
+            self.more_index.append([self.batch.add_sdf(s, m, c.sdf_dims) for (m, s), c in zip(pairs, o.more)])
+        for i, (h, si) in enumerate(zip(self.hair, self.sdf_index)):
             self.batch.add_hair(h, si)
+            for sj in self.more_index[i]:
+                self.batch.add_hair_collision(i, sj)
         self.batch.build()
         self.autotune_frames = autotune_frames
         self._tuned = autotune_frames <= 0
@@ -142,6 +169,9 @@ class BatchedPipeline(PlainPipeline):
             if si >= 0:
                 self.batch.set_sdf_frame(si, g, margin_world(o, g))
                 self.batch.set_mesh_bones(si, mb)
+            for sj, c, gm, mbm in zip(self.more_index[i], o.more, fin.more_grids[i], fin.more_bones[i]):
+                self.batch.set_sdf_frame(sj, gm, margin_world(c, gm))
+                self.batch.set_mesh_bones(sj, mbm)
 
     def run(self, fin: FrameInputs) -> None:
         if not self._tuned:

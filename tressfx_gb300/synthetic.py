@@ -258,6 +258,20 @@ def sample_on_ellipsoid(center, radii, count: int, rng: np.random.Generator, y_m
 
 # ---------------------------------------------------------------------------------------- scenes
 @dataclass
+class Collider:
+    """A further collision mesh of a hair object, collided after the object's first (SceneObject.mesh) and
+    its earlier further meshes: Simulation::RunCollision applies every collision mesh to every hair
+    object in turn (src/Simulation.cpp:106-118).  Same fields as the object's own mesh."""
+    mesh: Mesh
+    mesh_bone_fn: object
+    sdf_dims: tuple[int, int, int]
+    sdf_cell: float
+    sdf_center0: np.ndarray
+    follow_bone: int = 0
+    collision_margin_cells: float = 0.5
+
+
+@dataclass
 class SceneObject:
     asset: HairAsset
     settings: dict
@@ -269,6 +283,7 @@ class SceneObject:
     sdf_center0: np.ndarray | None = None   # initial grid centre
     follow_bone: int = 0              # bone whose motion moves the grid (TressFXBoneSkinning::GetBoundingBox)
     collision_margin_cells: float = 0.5
+    more: list = field(default_factory=list)   # further Colliders, in collision order (needs `mesh`)
 
 
 @dataclass
