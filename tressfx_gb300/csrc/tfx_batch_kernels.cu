@@ -162,15 +162,20 @@ __global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __r
 // One block runs one group of GS = fused_group_strands(N) guide strands of one object at a time.
 // Shared memory, strand-major rows of N vertices padded to N+1 float4, so that both the one-lane-per-
 // strand sweep and the one-lane-per-vertex passes are free of bank conflicts:
-//   TP[GS][N+1] positions   TI[GS][N+1] InitialPos, then the bind pose
+//   TP[GS][N+1] positions   TI[GS][N+1] InitialPos, then the bind pose (below N = 64 only)
 //   SK[GS][4] blended bone matrix rows   SL[GS][3] StrandLevelData
 //   one mbarrier, on which the bulk copies that bring a group's rows in complete.
 // Prev, Tangent and RestLength never enter shared memory: each thread reads (and writes) its own
 // vertices' words in global memory (coalesced), which keeps a block small enough for six to fit per
 // SM at n = 32 and 64, and the serial local-shape sweeps of that many groups to run side by side.
-__host__ __device__ constexpr int fused_group_strands(int n) { return n >= 64 ? 16 : 32; }
+// Below 64 vertices a strand's local-shape sweeps (as many as the settings ask, TressFXHairObject.cpp:
+// 402-411) read the bind pose from a second tile; at 64 a strand has one sweep a frame, which computes
+// the bind pose from InitialPos in global memory instead, so a group holds 32 strands in about the
+// shared memory 16 took with the tile, and twice as many strands sweep at once per SM.
+__host__ __device__ constexpr bool fused_init_tile(int n) { return n < 64; }
+__host__ __device__ constexpr int fused_group_strands(int) { return 32; }
 __host__ __device__ constexpr int fused_smem_for(int n) {
-    return 2 * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * 7 * 16 + 16;
+    return (fused_init_tile(n) ? 2 : 1) * fused_group_strands(n) * (n + 1) * 16 + fused_group_strands(n) * 7 * 16 + 16;
 }
 // k_fused_strands modes: the whole frame of the group, or its part before the local-shape sweeps
 // (integration, strand-level data, VSP; the state goes to global memory for k_local_sweep), or its
@@ -281,6 +286,32 @@ __device__ __forceinline__ void sweep_wavefront(float4* __restrict__ SP, const f
     }
 }
 
+// The one sweep of a strand at N = 64 (the shader's single sweep; more when the caller asks for more
+// dispatches, one after the other): as the single-sweep case of sweep_wavefront, with the bind pose of
+// vertex j computed here as qrot(skinning quaternion, InitialPos_j), exactly as phase 1b computes it
+// for the tile, and InitialPos loaded two steps ahead.
+template <int N>
+__device__ __forceinline__ void sweep_single_global(float4* __restrict__ P, const float4* __restrict__ init, Q4 bq,
+                                                    float stiff) {
+    auto bind = [&](float4 ip) { return qrot(bq, xyz(ip)); };
+    float4 pm1 = P[0], pos = P[1], next = P[2];
+    float3 bm1 = bind(__ldg(init + 0)), b0 = bind(__ldg(init + 1)), bnext = bind(__ldg(init + 2));
+    float4 ahead = __ldg(init + 3);
+    for (int j = 1; j <= N - 2; ++j) {
+        float4 pp1 = next;
+        const float3 bp1 = bnext;
+        if (j + 2 <= N - 1) {
+            next = P[j + 2];
+            bnext = bind(ahead);
+            if (j + 3 <= N - 1) ahead = __ldg(init + j + 3);
+        }
+        local_shape_step(pm1, pos, pp1, bm1, b0, bp1, stiff);
+        P[j] = pos;
+        pm1 = pos; pos = pp1; bm1 = b0; b0 = bp1;
+    }
+    P[N - 1] = pos;
+}
+
 // Register bounds: at n <= 16 the tiles are small (21 KB a block) and registers decide residency, so
 // 64 a thread (eight 4-warp blocks per SM; a few words spill) beat 80 (six blocks).
 template <int N, int VPL>
@@ -291,10 +322,11 @@ __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused
     constexpr int RS = N + 1;       // tile row stride, float4
     constexpr int L = N / VPL;      // lanes per strand in the per-strand passes
     constexpr int SPW = 32 / L;     // strands per warp pass
+    constexpr bool KI = fused_init_tile(N);   // InitialPos / bind-pose tile
     extern __shared__ float4 smem_f4[];
     float4* TP = smem_f4;
-    float4* TI = TP + GS * RS;
-    float4* SK = TI + GS * RS;
+    float4* TI = TP + GS * RS;      // used only when KI
+    float4* SK = TP + (KI ? 2 : 1) * GS * RS;
     float4* SL = SK + GS * 4;
     const uint32_t bar = smem_u32(SL + GS * 3);
 
@@ -321,14 +353,14 @@ __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused
         float4 bq4 = make_float4(0.f, 0.f, 0.f, 0.f);
         const bool pre = mode != kFusedPost, post = mode != kFusedPre;   // phases 0-2 / phase 3 run
         if (warp == 0) {
-            // rows: Pos always; InitialPos for phases 0-2
-            const uint32_t rowBytes = N * 16 + (pre ? N * 16 : 0);
+            // rows: Pos always; InitialPos for phases 0-2 when it has a tile
+            const uint32_t rowBytes = N * 16 + (pre && KI ? N * 16 : 0);
             if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)count * rowBytes);
             __syncwarp();
             if (lane < count) {
                 const size_t vo = (size_t)(gs0 + lane * (F + 1)) * N;
                 bulk_g2s(smem_u32(TP + lane * RS), h.pos + vo, N * 16, bar);
-                if (pre) bulk_g2s(smem_u32(TI + lane * RS), h.init + vo, N * 16, bar);
+                if (pre && KI) bulk_g2s(smem_u32(TI + lane * RS), h.init + vo, N * 16, bar);
             }
             if (pre && lane < count) {
                 // strand level, while the rows are in flight: the blended bone matrix and its quaternion
@@ -364,8 +396,9 @@ __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused
             float4 o0 = TP[s * RS], o1 = TP[s * RS + 1];
             const size_t vo = (size_t)gs * N;
             const float4 oo1 = h.prev[vo + 1];
-            const float4 n0 = integrate_vertex(c, m, TI[s * RS], o0, h.prev[vo], 0, N);
-            const float4 n1 = integrate_vertex(c, m, TI[s * RS + 1], o1, oo1, 1, N);
+            const float4 i0 = KI ? TI[s * RS] : __ldg(h.init + vo), i1 = KI ? TI[s * RS + 1] : __ldg(h.init + vo + 1);
+            const float4 n0 = integrate_vertex(c, m, i0, o0, h.prev[vo], 0, N);
+            const float4 n1 = integrate_vertex(c, m, i1, o1, oo1, 1, N);
             const float3 u = normalize(sub(xyz(o1), xyz(o0)));
             const float3 v = normalize(sub(xyz(n1), xyz(n0)));
             const Q4 rot = qfrom2(u, v);
@@ -397,7 +430,7 @@ __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused
                 m[r][0] = row.x; m[r][1] = row.y; m[r][2] = row.z; m[r][3] = row.w;
             }
             const size_t v = (size_t)(gs0 + s * (F + 1)) * N + j;
-            const float4 ip = TI[x], old = h.prev[v];
+            const float4 ip = KI ? TI[x] : __ldg(h.init + v), old = h.prev[v];
             float4 pv = TP[x];
             float4 p = integrate_vertex(c, m, ip, pv, old, j, N);
             h.prevprev[v] = old;
@@ -413,7 +446,7 @@ __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused
             }
             TP[x] = p;
             h.prev[v] = pv;   // read back by phase 3 (after a block barrier)
-            if (mode == kFusedFull) {   // the bind pose, for the sweeps below
+            if (KI && mode == kFusedFull) {   // the bind pose, for the sweeps below
                 const float4 b4 = SL[s * 3 + 0];
                 const float3 bp = qrot(Q4{b4.x, b4.y, b4.z, b4.w}, xyz(ip));
                 TI[x] = make_float4(bp.x, bp.y, bp.z, 0.0f);
@@ -434,11 +467,20 @@ __global__ void __launch_bounds__(256, N <= 16 ? 4 : (VPL <= 2 ? 3 : 2)) k_fused
         const int lsIters = mode == kFusedFull ? c->reserved0 : 0;
         if (lsIters > 0) {
             const float stiff = 0.5f * fminf(c->localStiffness, 0.95f);
-            for (int done = 0; done < lsIters;) {   // waves of up to one sweep per warp
-                const int KW = min(lsIters - done, nwarps);
-                if (warp < KW) sweep_wavefront<N>(TP, TI, lane, lane < count, warp, KW, stiff);
+            if constexpr (KI) {
+                for (int done = 0; done < lsIters;) {   // waves of up to one sweep per warp
+                    const int KW = min(lsIters - done, nwarps);
+                    if (warp < KW) sweep_wavefront<N>(TP, TI, lane, lane < count, warp, KW, stiff);
+                    __syncthreads();
+                    done += KW;
+                }
+            } else {
+                if (warp == 0 && lane < count) {
+                    const float4 b4 = SL[lane * 3 + 0];
+                    const float4* init = h.init + (size_t)(gs0 + lane * (F + 1)) * N;
+                    for (int k = 0; k < lsIters; ++k) sweep_single_global<N>(TP + lane * RS, init, Q4{b4.x, b4.y, b4.z, b4.w}, stiff);
+                }
                 __syncthreads();
-                done += KW;
             }
         }
 
