@@ -13,9 +13,9 @@
 //                           FloatFlip3 word.  The pairs and the encoding are the reference's, so the grid
 //                           is bit-identical.
 //  * k_fused_strands      - the six simulation stages of the guide strands (TressFXSimulation.hlsl:
-//                           609-975) for a group of guide strands (32, or 16 at n = 64) in one
-//                           pass.  Phase 0: bulk asynchronous copies (cp.async.bulk on an mbarrier)
-//                           bring the group's Pos and InitialPos rows into shared memory while warp 0
+//                           609-975) for a group of 32 guide strands in one pass.  Phase 0: bulk
+//                           asynchronous copies (cp.async.bulk on an mbarrier) bring the group's Pos
+//                           rows (and below n = 64 its InitialPos rows) into shared memory while warp 0
 //                           blends each strand's bone matrix.  Phase 1a
 //                           (one lane per strand): strand-level data.  Phase 1b (one thread per
 //                           vertex): integration + global shape, VSP, bind pose.  Phase 2 (one lane
