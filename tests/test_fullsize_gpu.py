@@ -75,3 +75,24 @@ def test_batched_full_size_dynamic_frames_autotuned(ctx, which):
         assert _moved(ora)
     finally:
         gpu.close()
+
+
+def test_batched_tiled_construct_full_size(ctx):
+    """The tile-binned SDF construct (TFX_BATCH_SDF_FORM 1) on the 64-object workload: every SDF and
+    every state buffer word for word against the oracle over six frames (four integrating)."""
+    sc = _scene("batched")
+    gpu = BatchedPipeline(ctx, sc, autotune_frames=0)
+    gpu.batch.set_option(gpu.batch.SDF_FORM, 1)
+    ora = OraclePipeline(sc)
+    try:
+        for f in range(6):
+            ora.step(gpu.step(f))
+        _compare(gpu, ora, "batched, tiled construct, frame 5")
+        for i, s in enumerate(gpu.sdfs):
+            got = s.read(int(np.prod(sc.objects[i].sdf_dims))).view(np.uint32)
+            want = np.ascontiguousarray(ora.sdf_words[i]).reshape(-1)[:got.size].view(np.uint32)
+            bad = np.nonzero(got != want)[0]
+            assert len(bad) == 0, f"SDF {i}: {len(bad)} of {got.size} cells differ (first {bad[:5].tolist()})"
+        assert _moved(ora)
+    finally:
+        gpu.close()
