@@ -5,8 +5,8 @@ simulation frame is below 2, TressFXHairObject.cpp:433-434): the positions are t
 and the Verlet term never runs.  These tests run 12 frames, so 10 of them integrate, and compare every
 state buffer of every object with the FP32 oracle word for word:
 
-* the plain path (one launch per object per stage) on the head (20,000 x 32, 4 follow hairs, SDF 64^3)
-  and fur (200,000 x 16, SDF 128^3) workloads;
+* the plain path (one launch per object per stage) on the head (20,000 x 32, 4 follow hairs, SDF 64^3),
+  fur (200,000 x 16, SDF 128^3) and 64-object workloads;
 * the batched path with the launch shapes its autotuner picks (as the benchmark runs it) on the head,
   fur and 64-object workloads.
 """
@@ -43,7 +43,7 @@ def _moved(ora) -> bool:
     return any(not np.array_equal(oh.pos, oh.init) for oh in ora.hair)
 
 
-@pytest.mark.parametrize("which", ["head", "fur"])
+@pytest.mark.parametrize("which", ["head", "fur", "batched"])
 def test_plain_full_size_dynamic_frames(ctx, which):
     sc = _scene(which)
     gpu = PlainPipeline(ctx, sc)
