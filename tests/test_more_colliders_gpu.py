@@ -103,3 +103,40 @@ def test_batch_rejects_bad_further_collisions(ctx):
         b.close()
         for x in (s, m, hair):
             x.close()
+
+
+def _mixed_scene():
+    """Four objects of different strand lengths (one with follow hairs); objects 0 and 2 collide with
+    two further meshes, object 3 with one, object 1 with none: the levels hold different objects."""
+    from tressfx_gb300.synthetic import scene_batched
+    sc = scene_batched(seed=12, num_objects=4, min_strands=256, max_strands=1200, verts=(8, 16, 32, 64),
+                       min_tris=1500, max_tris=3000, sdf_choices=(24, 32), follows=1, frames=FRAMES)
+    for k, extra in ((0, 2), (2, 2), (3, 1)):
+        o = sc.objects[k]
+        c = np.asarray(o.sdf_center0) + np.array([0.0, 0.1, 0.0])   # head centre, as the scene places it
+        for q in range(extra):
+            off = np.array([(0.07, -0.09, 0.06), (-0.08, -0.05, 0.03)][q])
+            m = _ellipsoid(c + off, (0.05, 0.05, 0.05), 1200)
+            p = m.vertices[:, :3]
+            ext = float((p.max(0) - p.min(0)).max()) + 0.04
+            o.more.append(Collider(m, o.mesh_bone_fn, (28, 28, 28), ext / 28, (p.min(0) + p.max(0)) / 2, follow_bone=2,
+                                   collision_margin_cells=0.5))
+    return sc
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", ["plain", "batched"])
+def test_several_collision_meshes_mixed_classes(ctx, path):
+    sc = _mixed_scene()
+    gpu = PlainPipeline(ctx, sc) if path == "plain" else BatchedPipeline(ctx, sc, autotune_frames=0)
+    ora = OraclePipeline(sc)
+    try:
+        for f in range(FRAMES):
+            if path == "plain":
+                gpu.step(f)
+                ora.step(FrameInputs(sc, f))
+            else:
+                ora.step(gpu.step(f))
+        _compare(gpu, ora, f"mixed classes, {path}, frame {FRAMES - 1}")
+    finally:
+        gpu.close()
