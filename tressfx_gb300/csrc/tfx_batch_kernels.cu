@@ -141,18 +141,26 @@ __global__ void __launch_bounds__(256) k_batch_sdf_expand(const BatchSdf* __rest
     }
 }
 
-// ConstructSignedDistanceField, :329-397, one warp per triangle.
-__global__ void __launch_bounds__(256) k_batch_sdf_construct(const BatchSdf* __restrict__ sdfs, int nsdf, int totalTris) {
-    const int warpsTotal = gridDim.x * (blockDim.x >> 5);
-    const int lane = threadIdx.x & 31;
-    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < totalTris; t += warpsTotal) {
-        const BatchSdf& s = sdfs[find_by_prefix_tri(sdfs, nsdf, t)];
-        const SdfGrid g = s.frame->grid;
-        const int tri = t - s.firstTriangle;
-        const float3 x0 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 0)));
-        const float3 x1 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 1)));
-        const float3 x2 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 2)));
-        sdf_construct_triangle_warp(s.words, g, x0, x1, x2, lane);
+// ConstructSignedDistanceField, :329-397.  Each warp takes chunks of `per` (<= 32) consecutive
+// triangles of the batch's triangle list (which may span SDFs): lane k finds the SDF of the chunk's
+// k-th triangle and makes its job, then the warp runs the triangles' cell loops in turn.
+// WARPS = warps per block; STAGED as in sdf_construct_chunk_warp.
+template <int WARPS, bool STAGED>
+__global__ void __launch_bounds__(WARPS * 32) k_batch_sdf_construct(const BatchSdf* __restrict__ sdfs, int nsdf,
+                                                                     int totalTris, int per) {
+    __shared__ TriJob jobs[STAGED ? WARPS : 1][STAGED ? kTriJobsPerWarp : 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunks = (totalTris + per - 1) / per;
+    for (int k = blockIdx.x * WARPS + warp; k < chunks; k += gridDim.x * WARPS) {
+        const int first = k * per;
+        sdf_construct_chunk_warp<STAGED>(jobs[STAGED ? warp : 0], first, min(per, totalTris - first), lane, [&](int t) {
+            const BatchSdf& s = sdfs[find_by_prefix_tri(sdfs, nsdf, t)];
+            const int tri = t - s.firstTriangle;
+            const float3 x0 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 0)));
+            const float3 x1 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 1)));
+            const float3 x2 = xyz(__ldg(s.mesh + 2 * (size_t)__ldg(s.indices + 3 * tri + 2)));
+            return tri_job(s.frame->grid, s.words, x0, x1, x2);
+        });
     }
 }
 
@@ -1220,9 +1228,23 @@ cudaError_t launch_batch_sdf(const SdfBatchLaunch& L, cudaStream_t s) {
     k_batch_sdf_init<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
     if (L.totalTris > 0) {
         const int warpsPerBlock = L.constructThreads / 32;
-        const long long blocks = (L.totalTris + warpsPerBlock - 1) / warpsPerBlock;
-        k_batch_sdf_construct<<<(unsigned)std::min<long long>(blocks, (long long)sm_count() * 64), L.constructThreads, 0, s>>>(
-            L.sdfs, L.nsdf, L.totalTris);
+        const int per = sdf_construct_chunk(L.totalTris, sm_count());
+        const long long chunks = ((long long)L.totalTris + per - 1) / per;
+        const unsigned blocks =
+            (unsigned)std::min<long long>((chunks + warpsPerBlock - 1) / warpsPerBlock, (long long)sm_count() * 64);
+        const bool staged = per >= kTriJobsStagedFrom;
+        if (warpsPerBlock == 2 && staged)
+            k_batch_sdf_construct<2, true><<<blocks, 64, 0, s>>>(L.sdfs, L.nsdf, L.totalTris, per);
+        else if (warpsPerBlock == 2)
+            k_batch_sdf_construct<2, false><<<blocks, 64, 0, s>>>(L.sdfs, L.nsdf, L.totalTris, per);
+        else if (warpsPerBlock == 8 && staged)
+            k_batch_sdf_construct<8, true><<<blocks, 256, 0, s>>>(L.sdfs, L.nsdf, L.totalTris, per);
+        else if (warpsPerBlock == 8)
+            k_batch_sdf_construct<8, false><<<blocks, 256, 0, s>>>(L.sdfs, L.nsdf, L.totalTris, per);
+        else if (staged)
+            k_batch_sdf_construct<4, true><<<blocks, 128, 0, s>>>(L.sdfs, L.nsdf, L.totalTris, per);
+        else
+            k_batch_sdf_construct<4, false><<<blocks, 128, 0, s>>>(L.sdfs, L.nsdf, L.totalTris, per);
     }
     k_batch_sdf_finalize<<<gq, 256, 0, s>>>(L.sdfs, L.nsdf, q);
     if (L.expand) return launch_batch_sdf_expand(L, s);

@@ -22,18 +22,25 @@ __global__ void __launch_bounds__(256) k_sdf_initialize(uint32_t* __restrict__ s
     for (long long i = (n4 << 2) + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells; i += stride) sdf[i] = v;
 }
 
-// ConstructSignedDistanceField, :329-397.  One warp per triangle (sdf_construct_triangle_warp); the
-// warps stride over the triangles.
+// ConstructSignedDistanceField, :329-397.  Each warp takes chunks of `per` (<= 32) consecutive
+// triangles (sdf_construct_chunk_warp: STAGED, lane k makes the job of the chunk's k-th triangle), then
+// runs the triangles' cell loops in turn; the warps stride over the chunks.
+template <bool STAGED>
 __global__ void __launch_bounds__(128) k_sdf_construct(uint32_t* __restrict__ sdf, SdfGrid g,
                                                        const float4* __restrict__ mesh,
-                                                       const uint32_t* __restrict__ idx, int ntri) {
+                                                       const uint32_t* __restrict__ idx, int ntri, int per) {
+    __shared__ TriJob jobs[STAGED ? 4 : 1][STAGED ? kTriJobsPerWarp : 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int warpsTotal = gridDim.x * (blockDim.x >> 5);
-    const int lane = threadIdx.x & 31;
-    for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < ntri; t += warpsTotal) {
-        const float3 x0 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 0)));
-        const float3 x1 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 1)));
-        const float3 x2 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 2)));
-        sdf_construct_triangle_warp(sdf, g, x0, x1, x2, lane);
+    const int chunks = (ntri + per - 1) / per;
+    for (int k = blockIdx.x * (blockDim.x >> 5) + warp; k < chunks; k += warpsTotal) {
+        const int first = k * per;
+        sdf_construct_chunk_warp<STAGED>(jobs[STAGED ? warp : 0], first, min(per, ntri - first), lane, [&](int t) {
+            const float3 x0 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 0)));
+            const float3 x1 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 1)));
+            const float3 x2 = xyz(__ldg(mesh + 2 * (size_t)__ldg(idx + 3 * t + 2)));
+            return tri_job(g, sdf, x0, x1, x2);
+        });
     }
 }
 
@@ -161,8 +168,13 @@ cudaError_t launch_sdf_initialize(uint32_t* sdf, int64_t cells, cudaStream_t s) 
 cudaError_t launch_sdf_construct(uint32_t* sdf, const SdfGrid& g, const float4* mesh, const uint32_t* idx, int ntri,
                                  cudaStream_t s) {
     if (ntri <= 0) return cudaSuccess;
-    k_sdf_construct<<<(unsigned)std::min<long long>(((long long)ntri + 3) / 4, (long long)sm_count() * 64), 128, 0, s>>>(sdf, g, mesh,
-                                                                                                 idx, ntri);
+    const int per = sdf_construct_chunk(ntri, sm_count());
+    const long long chunks = ((long long)ntri + per - 1) / per;
+    const unsigned blocks = (unsigned)std::min<long long>((chunks + 3) / 4, (long long)sm_count() * 64);
+    if (per >= kTriJobsStagedFrom)
+        k_sdf_construct<true><<<blocks, 128, 0, s>>>(sdf, g, mesh, idx, ntri, per);
+    else
+        k_sdf_construct<false><<<blocks, 128, 0, s>>>(sdf, g, mesh, idx, ntri, per);
     return cudaGetLastError();
 }
 

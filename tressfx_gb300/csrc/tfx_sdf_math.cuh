@@ -114,21 +114,65 @@ __device__ __forceinline__ void tri_cell_box(const SdfGrid& g, float3 t0, float3
     hi.x = max(0, min(hi.x + 1, g.nx - 1)); hi.y = max(0, min(hi.y + 1, g.ny - 1)); hi.z = max(0, min(hi.z + 1, g.nz - 1));
 }
 
-// ConstructSignedDistanceField (:329-397) for one triangle by one warp: the triangle's invariants once,
-// then the lanes over the reference's cell box, each with the same atomicMin on the FloatFlip3 word.
-// Box coordinates of cell c: (c + 0.5) / m lies at least 0.5 / m from an integer, and the float product
-// (c + 0.5) * (1 / m) is within (c / m) * 2^-23 of it, so its truncation is the integer quotient while
-// c < 2^22; larger boxes use integer division.
-__device__ __forceinline__ void sdf_construct_triangle_warp(uint32_t* __restrict__ words, const SdfGrid& g, float3 x0,
-                                                           float3 x1, float3 x2, int lane) {
+// What ConstructSignedDistanceField (:329-397) computes once per triangle: its invariants, the
+// reference's cell box and the grid that box indexes.  In the warp constructs lane k of a warp makes
+// the job of the k-th of 32 consecutive triangles, and the warp then runs the 32 cell loops one after
+// another, reading each job from shared memory.  So the per-triangle work (the vertex loads, six
+// divisions for the box, two square roots and six divisions for the invariants) is done once per
+// triangle instead of once per lane; every value is the same expression on the same inputs, so the
+// results do not change.  48 words, 16-byte aligned: a job moves as twelve 16-byte loads.
+struct alignas(16) TriJob {
+    TriPre P;                  // 33 words
+    float ox, oy, oz, cell;    // the grid
+    int gnx, gny;
+    int lox, loy, loz;         // the box: first cell, row length, slice size, cells
+    int nx, nxy, vol;
+    float inxy;                // 1 / nxy
+    uint32_t* words;
+};
+static_assert(sizeof(TriJob) == 192, "a triangle job is 48 words");
+
+// Warps of a construct block keep up to 32 jobs each in shared memory.
+constexpr int kTriJobsPerWarp = 32;
+
+// Triangles per warp chunk for a launch over `tris` triangles: 32 where there are enough of them for
+// four chunks per resident warp (about 24 warps per SM), fewer down to one per chunk for small meshes,
+// so that a launch still spreads over every SM.
+inline int sdf_construct_chunk(long long tris, int sms) {
+    const long long per = tris / ((long long)sms * 96);
+    return (int)(per < 1 ? 1 : per > kTriJobsPerWarp ? kTriJobsPerWarp : per);
+}
+// Chunks this small make their jobs in every lane instead (no shared memory, fewer registers): staging
+// a job through shared memory costs more than the few lanes it would spare.
+constexpr int kTriJobsStagedFrom = 4;
+
+__device__ __forceinline__ TriJob tri_job(const SdfGrid& g, uint32_t* words, float3 x0, float3 x1, float3 x2) {
+    TriJob J;
     int3 lo, hi;
     tri_cell_box(g, x0, x1, x2, lo, hi);
-    const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
-    const int nxy = nx * ny;
-    const int vol = nxy * nz;
-    const TriPre P = tri_pre(x0, x1, x2);
+    J.P = tri_pre(x0, x1, x2);
+    J.ox = g.ox; J.oy = g.oy; J.oz = g.oz; J.cell = g.cell;
+    J.gnx = g.nx; J.gny = g.ny;
+    J.lox = lo.x; J.loy = lo.y; J.loz = lo.z;
+    J.nx = hi.x - lo.x + 1;
+    J.nxy = J.nx * (hi.y - lo.y + 1);
+    J.vol = J.nxy * (hi.z - lo.z + 1);
+    J.inxy = 1.0f / (float)J.nxy;
+    J.words = words;
+    return J;
+}
+
+// The cell loop of one job by one warp: the lanes over the box, each with the reference's distance and
+// the same atomicMin on the FloatFlip3 word.  Box coordinates of cell c: (c + 0.5) / m lies at least
+// 0.5 / m from an integer, and the float product (c + 0.5) * (1 / m) is within (c / m) * 2^-23 of it,
+// so its truncation is the integer quotient while c < 2^22; larger boxes use integer division.
+__device__ __forceinline__ void sdf_construct_job_warp(const TriJob& J, int lane) {
+    SdfGrid g;
+    g.ox = J.ox; g.oy = J.oy; g.oz = J.oz; g.cell = J.cell;
+    g.nx = J.gnx; g.ny = J.gny; g.nz = 0; g.reserved = 0;
+    const int nx = J.nx, nxy = J.nxy, vol = J.vol;
     const bool floatIdx = vol < (1 << 22);
-    const float inxy = 1.0f / (float)nxy, inx = 1.0f / (float)nx;
+    const float inxy = J.inxy, inx = 1.0f / (float)nx;
     for (int c = lane; c < vol; c += 32) {
         int cz, r, cy;
         if (floatIdx) {
@@ -140,10 +184,30 @@ __device__ __forceinline__ void sdf_construct_triangle_warp(uint32_t* __restrict
             r = c - cz * nxy;
             cy = r / nx;
         }
-        const int x = lo.x + (r - cy * nx), y = lo.y + cy, z = lo.z + cz;
-        const float d = signed_dist_pre(sdf_cell_pos(g, x, y, z), P);
-        atomicMin(words + ((long long)z * g.ny + y) * g.nx + x, float_flip3(d));
+        const int x = J.lox + (r - cy * nx), y = J.loy + cy, z = J.loz + cz;
+        const float d = signed_dist_pre(sdf_cell_pos(g, x, y, z), J.P);
+        atomicMin(J.words + ((long long)z * g.ny + y) * g.nx + x, float_flip3(d));
     }
+}
+
+// One warp's chunk of `count` (<= 32) consecutive triangles starting at `first`.  STAGED: lane k makes
+// the job of triangle first + k with make(t) into `jobs`, the warp's own 32-job area, then the warp runs
+// the cell loops; the chunk ends with the warp synchronised, so the area can take the next chunk.
+// Otherwise every lane makes each job itself and `jobs` is not used.
+template <bool STAGED, class MakeJob>
+__device__ __forceinline__ void sdf_construct_chunk_warp(TriJob* __restrict__ jobs, int first, int count, int lane,
+                                                         MakeJob make) {
+    if (!STAGED) {
+        for (int j = 0; j < count; ++j) sdf_construct_job_warp(make(first + j), lane);
+        return;
+    }
+    if (lane < count) jobs[lane] = make(first + lane);
+    __syncwarp();
+    for (int j = 0; j < count; ++j) {
+        const TriJob J = jobs[j];
+        sdf_construct_job_warp(J, lane);
+    }
+    __syncwarp();
 }
 
 // GetSignedDistance + TrilinearInterpolate, :414-527
