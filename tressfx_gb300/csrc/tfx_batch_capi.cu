@@ -480,8 +480,8 @@ static int snapshot_restore(Snapshot& sn, cudaStream_t s) {
 }
 
 // Time per frame of the frame graph captured for the current shapes: the graph is uploaded and
-// launched twice untimed, then the mean over max(frames, 6) launches is taken twice and the smaller
-// kept (a freshly instantiated graph's first launches carry one-off costs).
+// launched twice untimed, then the mean over max(frames, 6) launches is taken three times and the
+// smallest kept (a freshly instantiated graph's first launches carry one-off costs).
 static int time_graph_frames(tfx_batch b, int frames, float* ms) {
     if (int r = capture_graphs(b)) return r;
     cudaStream_t s = b->ctx->stream;
@@ -492,7 +492,7 @@ static int time_graph_frames(tfx_batch b, int frames, float* ms) {
     cudaError_t e = cudaGraphUpload(b->graph[0], s);
     for (int w = 0; w < 2 && e == cudaSuccess; ++w) e = cudaGraphLaunch(b->graph[0], s);
     float best = 1e30f;
-    for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+    for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
         e = cudaEventRecord(e0, s);
         for (int f = 0; f < n && e == cudaSuccess; ++f) e = cudaGraphLaunch(b->graph[0], s);
         if (e == cudaSuccess) e = cudaEventRecord(e1, s);
