@@ -55,6 +55,26 @@ def test_batched_mixed_objects(ctx):
     run_pair(ctx, sc, 5)
 
 
+def test_batched_sdf_chunks_span_sdfs(ctx):
+    """Meshes of 20k-40k triangles: the batch's construct hands each warp chunks of several
+    consecutive triangles of the batch's list (on 152 SMs: 7 a chunk), which cross from one SDF's
+    triangles into the next; every grid and the hair state against the oracle."""
+    sc = scene_batched(seed=8, num_objects=4, min_strands=64, max_strands=256, min_tris=20000, max_tris=40000,
+                       sdf_choices=(48, 64), frames=3)
+    gpu = BatchedPipeline(ctx, sc)
+    ora = OraclePipeline(sc)
+    try:
+        for f in range(3):
+            fin = gpu.step(f)
+            ora.step(fin)
+        for i, g in enumerate(fin.grids):
+            assert np.array_equal(gpu.sdfs[i].read(g.num_cells), ora.sdf_words[i]), f"SDF {i}"
+        for i, (h, oh) in enumerate(zip(gpu.hair, ora.hair)):
+            assert_same(h, oh, f"object {i}")
+    finally:
+        gpu.close()
+
+
 def test_batched_autotune_keeps_state(ctx):
     sc = scene_batched(seed=6, num_objects=4, min_strands=64, max_strands=400, min_tris=800, max_tris=2000,
                        sdf_choices=(24, 32), frames=4)

@@ -1,7 +1,8 @@
 """The SDF build on meshes that are not smooth closed surfaces: random triangle soups, the same far from
 the origin, slivers, duplicated and coplanar overlapping triangles (ties of the atomicMin), tiny
-triangles, a fine grid over a dense mesh, and Construct alone on words already near its result --
-each grid bit for bit against the oracle."""
+triangles, a fine grid over a dense mesh, soups large enough that the construct's warps take chunks
+of several triangles (each lane making one triangle's job), and Construct alone on words already near
+its result -- each grid bit for bit against the oracle."""
 import numpy as np
 import pytest
 
@@ -97,6 +98,50 @@ def test_construct_fine_grid_dense_mesh(ctx):
         torch.cuda.synchronize()
         sdf.update(g)
         assert np.array_equal(sdf.read(cells), oracle.sdf_build(g, verts, idx.reshape(-1)))
+    finally:
+        sdf.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ntri", [70000, 480000])
+def test_construct_large_soup_in_chunks(ctx, ntri):
+    """A launch over this many triangles hands each warp chunks of several consecutive triangles (on
+    152 SMs: 4 a chunk at 70,000, 32 at 480,000); the soup mixes small triangles, exact duplicates,
+    coplanar overlaps and slivers, and its triangle count is not a multiple of the chunk."""
+    torch = pytest.importorskip("torch")
+    from tressfx_gb300.api import SDFCollision
+    rng = np.random.default_rng(ntri)
+    total = ntri - 3
+    ns, nd = total // 2, total // 8
+    a = rng.uniform(-0.1, 0.1, (ns, 3))
+    small = a[:, None, :] + rng.normal(0, 0.002, (ns, 3, 3))
+    dup = small[rng.integers(0, ns, nd)]                               # exact duplicates
+    cop = dup.copy()
+    cop[:, 2] = dup[:, 0] + 0.5 * (dup[:, 2] - dup[:, 0])              # coplanar, overlapping
+    b = rng.uniform(-0.1, 0.1, (total - ns - 2 * nd, 3))
+    d = rng.normal(0, 0.003, b.shape)
+    sliver = np.stack([b, b + d, b + rng.uniform(0, 1, (len(b), 1)) * d + rng.normal(0, 1e-7, b.shape)], 1)
+    tri = np.concatenate([small, dup, sliver, cop]).astype(np.float32)
+    assert len(tri) == total
+    verts = np.zeros((3 * len(tri), 8), np.float32)
+    verts[:, :3] = tri.reshape(-1, 3)
+    idx = np.arange(3 * len(tri), dtype=np.uint32).reshape(-1, 3)
+    p = verts[:, :3]
+    lo = p.min(0) - 0.01
+    cell = np.float32((p.max(0) - p.min(0)).max() / 96.0)
+    dims = tuple(int(x) for x in np.ceil((p.max(0) + 0.01 - lo) / cell) + 1)
+    g = _grid(lo, cell, dims)
+    cells = dims[0] * dims[1] * dims[2]
+    dv = torch.from_numpy(verts.reshape(-1)).cuda()
+    di = torch.from_numpy(idx.view(np.int32).reshape(-1)).cuda()
+    sdf = SDFCollision(ctx, cells)
+    try:
+        sdf.set_mesh_device(dv.data_ptr(), len(verts), di.data_ptr(), len(idx))
+        torch.cuda.synchronize()
+        sdf.update(g)
+        got = sdf.read(cells)
+        want = oracle.sdf_build(g, verts, idx.reshape(-1))
+        assert np.array_equal(got, want), f"{int((got != want).sum())} of {cells} cells differ"
     finally:
         sdf.close()
 

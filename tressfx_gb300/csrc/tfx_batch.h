@@ -93,6 +93,12 @@ struct SdfBatchLaunch {
     long long totalQuads;
     int constructThreads;
     int expand;      // some SDF keeps a corner-expanded copy: run the expansion
+    // the SDFs that keep one, so that the expansion runs over their cells only: their indices into
+    // `sdfs`, the prefix of their cell counts (nexp + 1 entries), and the sum
+    const int* expSdf;
+    const long long* expFirst;
+    int nexp;
+    long long expCells;
 };
 
 // The tiled SDF build (tfx_sdf_tiles.cu): triangles binned into 8x8x4-cell tiles, one block per tile

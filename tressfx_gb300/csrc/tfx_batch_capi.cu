@@ -75,6 +75,7 @@ struct tfx_batch_t {
     void* expandedArena = nullptr;   // corner-expanded copies of the SDF grids
     int expandMode = 2;              // TFX_BATCH_EXPANDED_GRIDS: 0 never, 1 always, 2 where lookups >= 4 per cell
     std::vector<float4*> sdfExpanded;   // per SDF: its slot in expandedArena
+    void* expTable = nullptr;        // SdfBatchLaunch::expSdf / expFirst
     BatchObject* objTable = nullptr;
     BatchMesh* meshTable = nullptr;
     BatchSdf* sdfTable = nullptr;
@@ -158,6 +159,7 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
     if (b->devBlock) cudaFree(b->devBlock);
     if (b->devArena) cudaFree(b->devArena);
     if (b->expandedArena) cudaFree(b->expandedArena);
+    if (b->expTable) cudaFree(b->expTable);
     if (b->tileArena) cudaFree(b->tileArena);
     for (auto t : b->levelPairs)
         if (t) cudaFree(t);
@@ -614,12 +616,27 @@ static int apply_expand_mode(tfx_batch b) {
     std::vector<BatchObject> objs(nobj);
     if (nsdf) TFX_CUDA(cudaMemcpy(sdfs.data(), b->sdfTable, sizeof(BatchSdf) * nsdf, cudaMemcpyDeviceToHost), "tfx_batch: SDFs");
     TFX_CUDA(cudaMemcpy(objs.data(), b->objTable, sizeof(BatchObject) * nobj, cudaMemcpyDeviceToHost), "tfx_batch: objects");
-    int any = 0;
+    std::vector<int> expSdf;
+    std::vector<long long> expFirst(1, 0);
     for (int i = 0; i < nsdf; ++i) {
         const double cells = (double)b->sdfDims[3 * i] * b->sdfDims[3 * i + 1] * b->sdfDims[3 * i + 2];
         const bool on = b->expandMode == 1 || (b->expandMode == 2 && lookups[i] >= 4.0 * cells);
         sdfs[i].expanded = on ? b->sdfExpanded[i] : nullptr;
-        any |= on ? 1 : 0;
+        if (on) {
+            expSdf.push_back(i);
+            expFirst.push_back(expFirst.back() + sdfs[i].numCells);
+        }
+    }
+    if (!b->expTable && nsdf > 0)
+        TFX_CUDA(cudaMalloc(&b->expTable, align256(sizeof(long long) * (size_t)(nsdf + 1)) + sizeof(int) * (size_t)nsdf),
+                 "tfx_batch: expansion table");
+    long long* devFirst = reinterpret_cast<long long*>(b->expTable);
+    int* devSdf = reinterpret_cast<int*>(reinterpret_cast<char*>(b->expTable) + align256(sizeof(long long) * (size_t)(nsdf + 1)));
+    if (!expSdf.empty()) {
+        TFX_CUDA(cudaMemcpy(devFirst, expFirst.data(), sizeof(long long) * expFirst.size(), cudaMemcpyHostToDevice),
+                 "tfx_batch: expansion table");
+        TFX_CUDA(cudaMemcpy(devSdf, expSdf.data(), sizeof(int) * expSdf.size(), cudaMemcpyHostToDevice),
+                 "tfx_batch: expansion table");
     }
     for (int o = 0; o < nobj; ++o) {
         const int si = b->hairSdf[o];
@@ -627,7 +644,11 @@ static int apply_expand_mode(tfx_batch b) {
     }
     if (nsdf) TFX_CUDA(cudaMemcpy(b->sdfTable, sdfs.data(), sizeof(BatchSdf) * nsdf, cudaMemcpyHostToDevice), "tfx_batch: SDFs");
     TFX_CUDA(cudaMemcpy(b->objTable, objs.data(), sizeof(BatchObject) * nobj, cudaMemcpyHostToDevice), "tfx_batch: objects");
-    b->sdfL.expand = any;
+    b->sdfL.expand = expSdf.empty() ? 0 : 1;
+    b->sdfL.expSdf = devSdf;
+    b->sdfL.expFirst = devFirst;
+    b->sdfL.nexp = (int)expSdf.size();
+    b->sdfL.expCells = expFirst.back();
     return TFX_OK;
 }
 
@@ -812,7 +833,7 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
     }
     if (nsdf > 0)
         TFX_CUDA(cudaMemcpy(b->sdfTable, sdfs.data(), sizeof(BatchSdf) * nsdf, cudaMemcpyHostToDevice), "tfx_batch: SDFs");
-    b->sdfL = SdfBatchLaunch{b->sdfTable, nsdf, firstTri, firstQuad, 128, 0};
+    b->sdfL = SdfBatchLaunch{b->sdfTable, nsdf, firstTri, firstQuad, 128, 0, nullptr, nullptr, 0, 0};
     b->expandMode = 2;
     if (int r = apply_expand_mode(b)) return r;
 

@@ -119,14 +119,21 @@ __global__ void __launch_bounds__(256) k_batch_sdf_finalize(const BatchSdf* __re
 // Corner-expanded copy of a finalized grid: record c holds the eight corners a trilinear lookup in
 // cell c reads, in TrilinearInterpolate's order ((x,y,z), (x+1,y,z), (x,y+1,z), (x+1,y+1,z), then the
 // same at z+1), so a lookup reads one 32-byte record instead of eight scattered words.  Only the
-// cells a lookup can use (x < nx-1, y < ny-1, z < nz-1) are written.
-__global__ void __launch_bounds__(256) k_batch_sdf_expand(const BatchSdf* __restrict__ sdfs, int nsdf,
-                                                          long long totalQuads) {
+// cells a lookup can use (x < nx-1, y < ny-1, z < nz-1) are written.  The threads run over the cells
+// of the SDFs that keep a copy (expSdf, with expFirst the prefix of their cell counts) and no others.
+__global__ void __launch_bounds__(256) k_batch_sdf_expand(const BatchSdf* __restrict__ sdfs,
+                                                          const int* __restrict__ expSdf,
+                                                          const long long* __restrict__ expFirst, int nexp,
+                                                          long long expCells) {
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 4 * totalQuads; t += stride) {
-        const BatchSdf& s = sdfs[find_by_prefix_quad(sdfs, nsdf, t >> 2)];
-        const long long c = t - 4 * s.firstQuad;
-        if (c >= s.numCells || !s.expanded) continue;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < expCells; t += stride) {
+        int lo = 0, hi = nexp - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(expFirst + mid) <= t) lo = mid; else hi = mid - 1;
+        }
+        const BatchSdf& s = sdfs[__ldg(expSdf + lo)];
+        const long long c = t - __ldg(expFirst + lo);
         const SdfGrid g = s.frame->grid;
         const long long nxy = (long long)g.nx * g.ny;
         const int z = (int)(c / nxy);
@@ -1252,10 +1259,9 @@ cudaError_t launch_batch_sdf(const SdfBatchLaunch& L, cudaStream_t s) {
 }
 
 cudaError_t launch_batch_sdf_expand(const SdfBatchLaunch& L, cudaStream_t s) {
-    if (L.nsdf <= 0 || !L.expand) return cudaSuccess;
-    const long long q = L.totalQuads;
-    const unsigned ge = (unsigned)std::min<long long>((4 * q + 255) / 256, (long long)sm_count() * 32);
-    k_batch_sdf_expand<<<ge, 256, 0, s>>>(L.sdfs, L.nsdf, q);
+    if (L.nsdf <= 0 || !L.expand || L.expCells <= 0) return cudaSuccess;
+    const unsigned ge = (unsigned)std::min<long long>((L.expCells + 255) / 256, (long long)sm_count() * 32);
+    k_batch_sdf_expand<<<ge, 256, 0, s>>>(L.sdfs, L.expSdf, L.expFirst, L.nexp, L.expCells);
     return cudaGetLastError();
 }
 
