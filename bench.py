@@ -190,14 +190,16 @@ def strand_bytes(scene) -> dict[int, float]:
 
 def follow_bytes(scene) -> dict[int, float]:
     """Algorithmic HBM bytes per frame of k_follow_collide for each n class: read the guide's Pos
-    and Tangent (32 B per guide vertex); per follow vertex read its inverse mass (4 B) and write Pos
-    and Tangent (32 B); per follow strand its root offset (16 B); every SDF cell once (4 B)."""
+    (16 B per guide vertex) and, with follow hairs, its Tangent (16 B); per follow vertex read its
+    inverse mass (4 B) and write Pos and Tangent (32 B); per follow strand its root offset (16 B);
+    every SDF cell once (4 B)."""
     out: dict[int, float] = {}
     for o in scene.objects:
         a = o.asset
         G, n, F = a.num_guide_strands, a.verts_per_strand, a.follow_per_guide
         cells = int(np.prod(o.sdf_dims)) if o.mesh is not None else 0
-        out[n] = out.get(n, 0.0) + 32 * G * n + 36 * F * G * n + 16 * F * G + 4 * cells
+        guide = 32 if F > 0 else 16
+        out[n] = out.get(n, 0.0) + guide * G * n + 36 * F * G * n + 16 * F * G + 4 * cells
     return out
 
 

@@ -816,7 +816,7 @@ __device__ __forceinline__ void follow_collide_vertex(const FollowGroup& fg, int
     const int gs = fg.firstStrand + s * (F + 1);
     const size_t vg = (size_t)gs * N + j;
     const float4 gp = h.pos[vg];
-    const float4 tn = h.tan[vg];
+    const float4 tn = F > 0 ? h.tan[vg] : make_float4(0.f, 0.f, 0.f, 0.f);   // copied to the follow vertices only
     const bool collide = sdf && j >= 2;
     const float factor = tip * ((float)j * kInvN) + 1.0f;
     for (int i = 0; i <= F; ++i) {
@@ -972,7 +972,10 @@ __global__ void __launch_bounds__(256, 4) k_follow_collide_queued(const BatchObj
             const int gs = fg.firstStrand + s * (F + 1);
             const size_t vg = (size_t)gs * N + j;
             float4 gp = make_float4(0.f, 0.f, 0.f, 0.f), tn = gp;
-            if (active) { gp = h.pos[vg]; tn = h.tan[vg]; }
+            if (active) {
+                gp = h.pos[vg];
+                if (F > 0) tn = h.tan[vg];   // copied to the follow vertices only
+            }
             const bool collide = active && fg.sdf && j >= 2;
             const float factor = fg.tip * ((float)j * kInvN) + 1.0f;
             for (int i = 0; i <= F; ++i) {
