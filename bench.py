@@ -32,6 +32,7 @@ e2e    = the same metric through the public C ABI with host buffers: every frame
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -142,6 +143,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class gc_paused:
+    """Holds the interpreter's garbage collector off inside the block (a collection pass first)."""
+
+    def __enter__(self):
+        gc.collect()
+        self.was = gc.isenabled()
+        gc.disable()
+        return self
+
+    def __exit__(self, *a):
+        if self.was:
+            gc.enable()
+
+
 def make_scene(name: str, objects: int = 64):
     from tressfx_gb300 import synthetic as S
     if name == "batched":
@@ -242,10 +257,11 @@ def run_plain(ctx, scene, steps: int, warmup: int) -> dict:
     ctx.synchronize()
     ctx.timestamps()
     # whole-frame device time without inner stamps
-    ctx.timestamp("start")
-    for f in range(warmup, warmup + steps):
-        frame(inputs[f], False)
-    ctx.timestamp("end")
+    with gc_paused():
+        ctx.timestamp("start")
+        for f in range(warmup, warmup + steps):
+            frame(inputs[f], False)
+        ctx.timestamp("end")
     st = ctx.timestamps()
     t_ms = st[-1][1] - st[0][1]
     # one more pass with stamps around every stage for the per-kernel split
@@ -320,12 +336,15 @@ def run_batched(ctx, scene, steps: int, warmup: int, device: int, autotune: int,
     ctx.synchronize()
     desc, launches = pipe.batch.describe()
 
-    # ---- exactly `steps` timed frames (device time)
+    # ---- exactly `steps` timed frames (device time); the interpreter's garbage collector is held off
+    # while frames are issued, as a pause of the issuing thread longer than the queued frames would
+    # leave the GPU waiting
     ctx.timestamps()
-    ctx.timestamp("start")
-    for _ in range(steps):
-        pipe.set_inputs(inputs[f % nframes]); pipe.run(inputs[f % nframes]); f += 1
-    ctx.timestamp("end")
+    with gc_paused():
+        ctx.timestamp("start")
+        for _ in range(steps):
+            pipe.set_inputs(inputs[f % nframes]); pipe.run(inputs[f % nframes]); f += 1
+        ctx.timestamp("end")
     st = ctx.timestamps()
     t_ms = st[-1][1] - st[0][1]
 
@@ -361,19 +380,20 @@ def run_batched(ctx, scene, steps: int, warmup: int, device: int, autotune: int,
         if o.mesh is not None:
             h2d += 48 + 64 * 3
     ctx.synchronize()
-    t0 = time.perf_counter()
-    prev = None
-    for k in range(steps):
-        fin = inputs[f % nframes]
-        pipe.set_inputs(fin)
-        pipe.run(fin)
-        ticket = pipe.batch.readback(ptrs[k % 2], pipe.batch.READBACK_XYZ)
-        if prev is not None:
-            pipe.batch.wait_readback(prev)   # frame k - 1's positions are in host memory
-        prev = ticket
-        f += 1
-    pipe.batch.wait_readback(prev)
-    e2e_s = time.perf_counter() - t0
+    with gc_paused():
+        t0 = time.perf_counter()
+        prev = None
+        for k in range(steps):
+            fin = inputs[f % nframes]
+            pipe.set_inputs(fin)
+            pipe.run(fin)
+            ticket = pipe.batch.readback(ptrs[k % 2], pipe.batch.READBACK_XYZ)
+            if prev is not None:
+                pipe.batch.wait_readback(prev)   # frame k - 1's positions are in host memory
+            prev = ticket
+            f += 1
+        pipe.batch.wait_readback(prev)
+        e2e_s = time.perf_counter() - t0
     last = pinned[(steps - 1) % 2][0].array.copy()
     dev = np.ascontiguousarray(pipe.hair[0].read(A.BUF_POSITIONS).reshape(-1, 4)[:, :3])
     assert np.array_equal(last.view(np.uint32), dev.view(np.uint32)), "readback differs from the device buffer"

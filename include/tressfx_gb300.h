@@ -416,7 +416,8 @@ int tfx_batch_set_hair_constants(tfx_batch batch, int index, const tfx_sim_param
 int tfx_batch_set_sdf_frame(tfx_batch batch, int index, const tfx_sdf_grid* grid, float margin_world);
 /* This frame's bone matrices of the collision mesh of SDF `index`. */
 int tfx_batch_set_mesh_bones(tfx_batch batch, int index, const float* bone_matrices, int num_bones);
-/* Launches one frame on the context's stream (asynchronous). */
+/* Launches one frame on the context's stream (asynchronous).  Up to eight frames may be queued: the
+ * call blocks only while the frame queued eight calls earlier is still running. */
 int tfx_batch_run(tfx_batch batch);
 /* Waits until every frame queued by tfx_batch_run has executed.  Returns TFX_ERR_TIMEOUT, once, if one
  * of them had a strand block give up its bounded wait (tfx_batch_run itself reports it when it next

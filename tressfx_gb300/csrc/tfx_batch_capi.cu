@@ -44,6 +44,9 @@ struct BatchClass {
     int numItems = 0;
 };
 
+// Frames tfx_batch_run can queue ahead of the GPU (pinned frame blocks and graph instances).
+constexpr int kFrameSlots = 8;
+
 struct tfx_batch_t {
     tfx_context ctx = nullptr;
     std::vector<tfx_hair> hairs;
@@ -64,10 +67,13 @@ struct tfx_batch_t {
     std::vector<size_t> objOff, sdfOff, meshOff;
     std::vector<int> objBones, meshBones;
     std::vector<char> staging;
-    char* pinned[2] = {nullptr, nullptr};
+    // kFrameSlots frame blocks in pinned memory, each with its graph instance: tfx_batch_run may run
+    // that many frames ahead of the GPU, so a pause of the calling thread shorter than the frames
+    // already queued leaves the GPU busy
+    char* pinned[kFrameSlots] = {};
     char* devBlock = nullptr;
-    cudaEvent_t done[2] = {nullptr, nullptr};
-    bool used[2] = {false, false};
+    cudaEvent_t done[kFrameSlots] = {};
+    bool used[kFrameSlots] = {};
     int slot = 0;
 
     // device tables
@@ -94,7 +100,7 @@ struct tfx_batch_t {
     int* pinnedErr = nullptr;   // its copy at the end of each frame, one word per slot
     int waitPolls = kFusedWaitPollsDefault;   // TFX_BATCH_WAIT_POLLS
 
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[kFrameSlots] = {};
     int launchesPerFrame = 0;
     std::string description;
 
@@ -121,7 +127,7 @@ static int report_timeout(tfx_batch b) {
     cudaError_t e = cudaStreamSynchronize(b->ctx->stream);
     if (e == cudaSuccess) e = cudaMemset(b->devErr, 0, sizeof(int));
     if (e != cudaSuccess) return cuda_fail(e, "tfx_batch: clearing the error flag");
-    b->pinnedErr[0] = b->pinnedErr[1] = 0;
+    for (int i = 0; i < kFrameSlots; ++i) b->pinnedErr[i] = 0;
     return fail(TFX_ERR_TIMEOUT, "tfx_batch: a fused strand block gave up waiting for its bulk copies");
 }
 
@@ -139,7 +145,7 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
     if (!b) return TFX_OK;
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kFrameSlots; ++i) {
         if (b->graph[i]) cudaGraphExecDestroy(b->graph[i]);
         if (b->pinned[i]) cudaFreeHost(b->pinned[i]);
         if (b->done[i]) cudaEventDestroy(b->done[i]);
@@ -407,7 +413,7 @@ static int launch_frame_forked(tfx_batch b, cudaStream_t s) {
 
 static int capture_graphs(tfx_batch b) {
     cudaStream_t s = b->ctx->stream;
-    for (int slot = 0; slot < 2; ++slot) {
+    for (int slot = 0; slot < kFrameSlots; ++slot) {
         if (b->graph[slot]) { cudaGraphExecDestroy(b->graph[slot]); b->graph[slot] = nullptr; }
         cudaGraph_t g = nullptr;
         TFX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
@@ -519,7 +525,7 @@ static int time_graph_frames(tfx_batch b, int frames, float* ms) {
 // form of the follow/collide kernel.
 static int autotune(tfx_batch b, int frames) {
     cudaStream_t s = b->ctx->stream;
-    for (int i = 0; i < 2; ++i) std::memcpy(b->pinned[i], b->staging.data(), b->blockBytes);
+    for (int i = 0; i < kFrameSlots; ++i) std::memcpy(b->pinned[i], b->staging.data(), b->blockBytes);
     Snapshot sn;
     if (int r = snapshot_take(b, sn, s)) return r;
     int rc = TFX_OK;
@@ -678,7 +684,7 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
     }
     b->blockBytes = std::max<size_t>(off, 16);
     b->staging.assign(b->blockBytes, 0);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kFrameSlots; ++i) {
         TFX_CUDA(cudaMallocHost((void**)&b->pinned[i], b->blockBytes), "tfx_batch: pinned frame block");
         TFX_CUDA(cudaEventCreateWithFlags(&b->done[i], cudaEventDisableTiming), "cudaEventCreate");
     }
@@ -700,11 +706,11 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
     b->sdfTable = (BatchSdf*)p; p += align256(sizes[2]);
     b->devErr = (int*)p;
     TFX_CUDA(cudaMemset(b->devErr, 0, sizeof(int)), "tfx_batch: clear error flag");
-    TFX_CUDA(cudaMallocHost((void**)&b->pinnedErr, 2 * sizeof(int)), "tfx_batch: pinned error flag");
+    TFX_CUDA(cudaMallocHost((void**)&b->pinnedErr, kFrameSlots * sizeof(int)), "tfx_batch: pinned error flag");
     TFX_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking), "tfx_batch: side stream");
     TFX_CUDA(cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming), "cudaEventCreate");
     TFX_CUDA(cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming), "cudaEventCreate");
-    b->pinnedErr[0] = b->pinnedErr[1] = 0;
+    for (int i = 0; i < kFrameSlots; ++i) b->pinnedErr[i] = 0;
 
     // corner-expanded grids: 8 floats per cell, at the SDF's quad prefix
     std::vector<long long> sdfFirstQuad(nsdf, 0);
@@ -929,7 +935,7 @@ static int check_runnable(tfx_batch b, const char* who) {
 // Claims the next pinned block: waits until its previous upload has executed, then fills it.
 static int claim_block(tfx_batch b, int* slotOut) {
     const int s = b->slot;
-    b->slot ^= 1;
+    b->slot = (s + 1) % kFrameSlots;
     if (b->used[s]) {
         TFX_CUDA(cudaEventSynchronize(b->done[s]), "cudaEventSynchronize");
         if (b->pinnedErr[s]) {
@@ -957,7 +963,7 @@ extern "C" int tfx_batch_synchronize(tfx_batch b) {
     if (!b || !b->built) return fail(TFX_ERR_INVALID_ARGUMENT, "tfx_batch_synchronize: batch not built");
     TFX_CUDA(cudaSetDevice(b->ctx->device), "cudaSetDevice");
     TFX_CUDA(cudaStreamSynchronize(b->ctx->stream), "cudaStreamSynchronize");
-    for (int s = 0; s < 2; ++s)
+    for (int s = 0; s < kFrameSlots; ++s)
         if (b->used[s] && b->pinnedErr[s]) return report_timeout(b);
     return TFX_OK;
 }
