@@ -367,7 +367,10 @@ typedef enum tfx_batch_option {
     TFX_BATCH_EXPANDED_GRIDS = 1,   /* collision lookups on a corner-expanded copy of an SDF (8 corners
                                        per cell): 0 never, 1 always, 2 (default) for the SDFs whose
                                        objects make at least 4 lookups per cell each frame          */
-    TFX_BATCH_OVERLAP_SDF = 2,      /* 1: the SDF build runs concurrently with the strand kernels    */
+    TFX_BATCH_OVERLAP_SDF = 2,      /* 1 (default): the SDF build runs concurrently with the strand
+                                       kernels, and each vertices-per-strand class (its strand and
+                                       follow/collide kernels) is a concurrent branch of its own;
+                                       0: one kernel after another                                   */
     TFX_BATCH_SDF_BLOCK = 3,        /* threads per block of the SDF construct: 64, 128 or 256         */
     TFX_BATCH_SPLIT_SWEEPS = 4,     /* 1: the local-shape sweeps run as their own launch (a thread per
                                        strand, up to four sweeps pipelined in registers) between two

@@ -84,6 +84,7 @@ struct FollowLaunch {
     int numItems;
     int chunks;      // chunks per work item (1 .. follow_max_chunks_per_item(n))
     int queued;      // 0 k_follow_collide; 1 k_follow_collide_queued (both stages queued); 2 (gradient stage queued)
+    int noFollow;    // every object of the class has no follow hairs: the kernels specialised for F = 0
 };
 
 struct SdfBatchLaunch {
@@ -146,6 +147,6 @@ int fused_smem_bytes(int n, int vpl, int warps);
 int fused_blocks_per_sm(int n, int vpl, int warps);
 int fused_group_size(int n);
 int follow_max_chunks_per_item(int n);   // 256-vertex chunks a work item can be cut into
-int follow_blocks_per_sm(int n, int mode);   // mode: FollowLaunch::queued
+int follow_blocks_per_sm(int n, int mode, bool noFollow);   // mode: FollowLaunch::queued
 
 }  // namespace tfx

@@ -39,6 +39,7 @@ struct BatchClass {
                                  // class has follow hairs, else 2 at n >= 64 (long strands: lanes of one warp
                                  // reach both surface and far vertices), else 0; the autotuner tries the others
     bool splitSweeps = false;    // local-shape sweeps in k_local_sweep between two strand passes
+    bool noFollow = false;       // no object of the class has follow hairs
     std::vector<WorkItem> hostItems;
     WorkItem* items = nullptr;  // device
     int numItems = 0;
@@ -96,6 +97,10 @@ struct tfx_batch_t {
     cudaStream_t side = nullptr;             // second capture branch: mesh skinning + SDF build
     bool overlap = true;                     // capture the SDF branch on `side`
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    // with `overlap`, each n class's strand and follow/collide kernels form their own branch too (the
+    // classes touch disjoint objects), so one class's last blocks run beside the next class's
+    cudaStream_t classStream[5] = {};
+    cudaEvent_t evClasses = nullptr, evClassDone[5] = {};
     int* devErr = nullptr;      // fused kernel: a block gave up waiting for its bulk copies
     int* pinnedErr = nullptr;   // its copy at the end of each frame, one word per slot
     int waitPolls = kFusedWaitPollsDefault;   // TFX_BATCH_WAIT_POLLS
@@ -162,6 +167,11 @@ extern "C" int tfx_batch_destroy(tfx_batch b) {
     if (b->evFork) cudaEventDestroy(b->evFork);
     if (b->evJoin) cudaEventDestroy(b->evJoin);
     if (b->side) cudaStreamDestroy(b->side);
+    for (int i = 0; i < 5; ++i) {
+        if (b->classStream[i]) cudaStreamDestroy(b->classStream[i]);
+        if (b->evClassDone[i]) cudaEventDestroy(b->evClassDone[i]);
+    }
+    if (b->evClasses) cudaEventDestroy(b->evClasses);
     if (b->devBlock) cudaFree(b->devBlock);
     if (b->devArena) cudaFree(b->devArena);
     if (b->expandedArena) cudaFree(b->expandedArena);
@@ -259,10 +269,11 @@ static void describe(tfx_batch b) {
 static void make_items(tfx_batch b, BatchClass& c) {
     c.hostItems.clear();
     c.followMode = c.n >= 64 ? 2 : 0;
+    c.noFollow = true;
     for (int o = 0; o < (int)b->hairs.size(); ++o) {
         tfx_hair h = b->hairs[o];
         if (h->n != c.n) continue;
-        if (h->F > 0) c.followMode = 1;
+        if (h->F > 0) { c.followMode = 1; c.noFollow = false; }
         const int gsz = fused_group_size(c.n);
         for (int g = 0; g < h->G; g += gsz) c.hostItems.push_back(WorkItem{o, g, std::min(gsz, h->G - g), 0});
     }
@@ -286,7 +297,7 @@ static int size_class(tfx_batch b, BatchClass& c) {
     if (c.perSMCap > 0) perSM = std::min(perSM, c.perSMCap);
     c.blocks = std::max(1, std::min(perSM * b->ctx->numSMs, c.numItems));
     // follow/collide: whole groups when every resident block gets at least four, else the smallest chunks
-    const int fResident = std::max(1, follow_blocks_per_sm(c.n, c.followMode)) * b->ctx->numSMs;
+    const int fResident = std::max(1, follow_blocks_per_sm(c.n, c.followMode, c.noFollow)) * b->ctx->numSMs;
     c.followChunks = c.numItems >= 4 * fResident ? 1 : follow_max_chunks_per_item(c.n);
     c.followBlocks = std::max(1, std::min(fResident, c.numItems * c.followChunks));
     return TFX_OK;
@@ -326,7 +337,8 @@ static int launch_strands(tfx_batch b, BatchClass& c, cudaStream_t s) {
 }
 
 static int launch_follows(tfx_batch b, BatchClass& c, cudaStream_t s) {
-    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems, c.followChunks, c.followMode};
+    FollowLaunch fl{c.n, c.followBlocks, b->objTable, c.items, c.numItems, c.followChunks, c.followMode,
+                    c.noFollow ? 1 : 0};
     cudaError_t e = launch_follow_collide(fl, s);
     return e == cudaSuccess ? TFX_OK : cuda_fail(e, "tfx_batch: follow/collide launch");
 }
@@ -391,6 +403,8 @@ static int launch_frame_direct(tfx_batch b, cudaStream_t s, std::vector<float>* 
 
 // The frame body as captured into the graph: the SDF branch (mesh skinning + SDF build) on the side
 // stream runs concurrently with the strand kernels, which need no SDF; k_follow_collide waits for both.
+// With `overlap` every n class is a branch of its own (its strand kernel, then, once the SDFs are
+// built, its follow/collide kernel); the further-mesh levels follow all of them.
 static int launch_frame_forked(tfx_batch b, cudaStream_t s) {
     const bool fork = b->overlap && b->side && !b->sdfs.empty();
     if (fork) {
@@ -401,13 +415,29 @@ static int launch_frame_forked(tfx_batch b, cudaStream_t s) {
     } else if (int r = launch_sdf_part(b, s)) {
         return r;
     }
-    for (auto& c : b->classes)
-        if (c.numItems > 0)
-            if (int r = launch_strands(b, c, s)) return r;
-    if (fork) TFX_CUDA(cudaStreamWaitEvent(s, b->evJoin, 0), "tfx_batch: join");
-    for (auto& c : b->classes)
-        if (c.numItems > 0)
-            if (int r = launch_follows(b, c, s)) return r;
+    if (!b->overlap) {
+        for (auto& c : b->classes)
+            if (c.numItems > 0)
+                if (int r = launch_strands(b, c, s)) return r;
+        for (auto& c : b->classes)
+            if (c.numItems > 0)
+                if (int r = launch_follows(b, c, s)) return r;
+        return launch_collide_levels(b, s);
+    }
+    TFX_CUDA(cudaEventRecord(b->evClasses, s), "tfx_batch: class fork");
+    int k = 0;
+    for (auto& c : b->classes) {
+        if (c.numItems == 0) continue;
+        cudaStream_t cs = k == 0 ? s : b->classStream[k];
+        if (k > 0) TFX_CUDA(cudaStreamWaitEvent(cs, b->evClasses, 0), "tfx_batch: class fork");
+        if (int r = launch_strands(b, c, cs)) return r;
+        if (fork) TFX_CUDA(cudaStreamWaitEvent(cs, b->evJoin, 0), "tfx_batch: join");
+        if (int r = launch_follows(b, c, cs)) return r;
+        if (k > 0) TFX_CUDA(cudaEventRecord(b->evClassDone[k], cs), "tfx_batch: class join");
+        ++k;
+    }
+    if (k == 0 && fork) TFX_CUDA(cudaStreamWaitEvent(s, b->evJoin, 0), "tfx_batch: join");
+    for (int i = 1; i < k; ++i) TFX_CUDA(cudaStreamWaitEvent(s, b->evClassDone[i], 0), "tfx_batch: class join");
     return launch_collide_levels(b, s);
 }
 
@@ -708,6 +738,11 @@ extern "C" int tfx_batch_build(tfx_batch b, int reserved) {
     TFX_CUDA(cudaMemset(b->devErr, 0, sizeof(int)), "tfx_batch: clear error flag");
     TFX_CUDA(cudaMallocHost((void**)&b->pinnedErr, kFrameSlots * sizeof(int)), "tfx_batch: pinned error flag");
     TFX_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking), "tfx_batch: side stream");
+    for (int i = 0; i < 5; ++i) {
+        TFX_CUDA(cudaStreamCreateWithFlags(&b->classStream[i], cudaStreamNonBlocking), "tfx_batch: class stream");
+        TFX_CUDA(cudaEventCreateWithFlags(&b->evClassDone[i], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    TFX_CUDA(cudaEventCreateWithFlags(&b->evClasses, cudaEventDisableTiming), "cudaEventCreate");
     TFX_CUDA(cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming), "cudaEventCreate");
     TFX_CUDA(cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming), "cudaEventCreate");
     for (int i = 0; i < kFrameSlots; ++i) b->pinnedErr[i] = 0;

@@ -802,12 +802,13 @@ __device__ __forceinline__ bool follow_group(const BatchObject& ob, const WorkIt
     return true;
 }
 
-// Guide vertex e of a group: its follow vertices and the collision of all of them.
-template <int N>
+// Guide vertex e of a group: its follow vertices and the collision of all of them.  NF: every object
+// of the class has no follow hairs (F = 0 known at compile time, which frees registers).
+template <int N, bool NF>
 __device__ __forceinline__ void follow_collide_vertex(const FollowGroup& fg, int e) {
     constexpr float kInvN = 1.0f / (float)N;   // exact: N is a power of two, so j * kInvN == j / N
     const HairView& h = fg.h;
-    const int F = h.F;
+    const int F = NF ? 0 : h.F;
     const float* __restrict__ sdf = fg.sdf;
     const float4* __restrict__ sdf8 = fg.sdf8;
     const SdfGrid& sg = fg.sg;
@@ -858,8 +859,8 @@ __device__ __forceinline__ void follow_collide_vertex(const FollowGroup& fg, int
 // is cut into chunksPerItem chunks of guide vertices (a multiple of 256), which persistent blocks take
 // in turn: with few groups per block, smaller chunks spread groups of unequal cost (collisions) evenly
 // over the SMs; with many, whole groups keep the per-chunk overhead low.
-template <int N>
-__global__ void __launch_bounds__(256, 4) k_follow_collide(const BatchObject* __restrict__ objs,
+template <int N, bool NF>
+__global__ void __launch_bounds__(256, NF ? 5 : 4) k_follow_collide(const BatchObject* __restrict__ objs,
                                                            const WorkItem* __restrict__ items, int numItems,
                                                            int chunksPerItem) {
     constexpr int kGroupVerts = fused_group_strands(N) * N;
@@ -872,7 +873,7 @@ __global__ void __launch_bounds__(256, 4) k_follow_collide(const BatchObject* __
         const int end = min(begin + chunkLen, wi.count * N);
         FollowGroup fg;
         if (!follow_group(objs[wi.obj], wi, fg)) continue;
-        for (int e = begin + (int)threadIdx.x; e < end; e += blockDim.x) follow_collide_vertex<N>(fg, e);
+        for (int e = begin + (int)threadIdx.x; e < end; e += blockDim.x) follow_collide_vertex<N, NF>(fg, e);
     }
 }
 
@@ -943,8 +944,8 @@ __device__ __forceinline__ void follow_stage1(const FollowGroup& fg, size_t vbas
 
 // QueueFirst = false: each lane runs its vertices' first lookup itself and only the vertices within
 // the margin are queued (for classes without follow hairs, where a lane has one vertex per step).
-template <int N, bool QueueFirst>
-__global__ void __launch_bounds__(256, 4) k_follow_collide_queued(const BatchObject* __restrict__ objs,
+template <int N, bool QueueFirst, bool NF>
+__global__ void __launch_bounds__(256, NF ? 5 : 4) k_follow_collide_queued(const BatchObject* __restrict__ objs,
                                                                   const WorkItem* __restrict__ items, int numItems,
                                                                   int chunksPerItem) {
     constexpr int kGroupVerts = fused_group_strands(N) * N;
@@ -962,7 +963,7 @@ __global__ void __launch_bounds__(256, 4) k_follow_collide_queued(const BatchObj
         FollowGroup fg;
         if (!follow_group(objs[wi.obj], wi, fg)) continue;
         const HairView& h = fg.h;
-        const int F = h.F;
+        const int F = NF ? 0 : h.F;
         const size_t vbase = (size_t)fg.firstStrand * N;
         int n1 = 0, n2 = 0;
         for (int base = begin + warp * 32; base < end; base += blockDim.x) {
@@ -1143,35 +1144,43 @@ int fused_blocks_per_sm(int n, int vpl, int warps) {
 
 int follow_max_chunks_per_item(int n) { return (fused_group_strands(n) * n + 255) / 256; }
 
-template <int N>
-static cudaError_t launch_follow_n(const FollowLaunch& fl, cudaStream_t s) {
+template <int N, bool NF>
+static cudaError_t launch_follow_nf(const FollowLaunch& fl, cudaStream_t s) {
     if (fl.queued == 1)
-        k_follow_collide_queued<N, true><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+        k_follow_collide_queued<N, true, NF><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
     else if (fl.queued == 2)
-        k_follow_collide_queued<N, false><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+        k_follow_collide_queued<N, false, NF><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
     else
-        k_follow_collide<N><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
+        k_follow_collide<N, NF><<<fl.blocks, 256, 0, s>>>(fl.objs, fl.items, fl.numItems, fl.chunks);
     return cudaGetLastError();
 }
 
-int follow_blocks_per_sm(int n, int mode) {
-    int nb = 0;
-    cudaError_t e = cudaErrorInvalidValue;
-#define TFX_FOLLOW_OCC(NN)                                                                                            \
-    case NN:                                                                                                          \
-        e = mode == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide_queued<NN, true>, 256, 0)  \
-            : mode == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide_queued<NN, false>, 256, 0) \
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_follow_collide<NN>, 256, 0);            \
-        break;
+template <int N>
+static cudaError_t launch_follow_n(const FollowLaunch& fl, cudaStream_t s) {
+    return fl.noFollow ? launch_follow_nf<N, true>(fl, s) : launch_follow_nf<N, false>(fl, s);
+}
+
+template <bool NF>
+static cudaError_t follow_occupancy(int n, int mode, int* nb) {
+#define TFX_FOLLOW_OCC(NN)                                                                                                \
+    case NN:                                                                                                              \
+        return mode == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, k_follow_collide_queued<NN, true, NF>, 256, 0)  \
+               : mode == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, k_follow_collide_queued<NN, false, NF>, 256, 0) \
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, k_follow_collide<NN, NF>, 256, 0);
     switch (n) {
         TFX_FOLLOW_OCC(4)
         TFX_FOLLOW_OCC(8)
         TFX_FOLLOW_OCC(16)
         TFX_FOLLOW_OCC(32)
         TFX_FOLLOW_OCC(64)
-        default: break;
+        default: return cudaErrorInvalidValue;
     }
 #undef TFX_FOLLOW_OCC
+}
+
+int follow_blocks_per_sm(int n, int mode, bool noFollow) {
+    int nb = 0;
+    const cudaError_t e = noFollow ? follow_occupancy<true>(n, mode, &nb) : follow_occupancy<false>(n, mode, &nb);
     return e == cudaSuccess ? nb : 0;
 }
 
