@@ -75,6 +75,35 @@ def test_batched_sdf_chunks_span_sdfs(ctx):
         gpu.close()
 
 
+@pytest.mark.parametrize("form", [0, 1, 2])
+def test_batched_classes_with_and_without_follow_hairs(ctx, form):
+    """A class whose objects have no follow hairs runs the follow/collide kernels specialised for
+    F = 0; a class mixing objects with and without follow hairs runs the general ones.  Both, in each
+    follow/collide form, against the oracle."""
+    from tressfx_gb300.synthetic import build_asset
+    sc = scene_batched(seed=9, num_objects=6, min_strands=64, max_strands=300, min_tris=800, max_tris=2000,
+                       sdf_choices=(24, 32), verts=(16, 32), frames=4)
+    rng = np.random.default_rng(90)
+    for o in sc.objects[2:4]:   # two of the three n = 16 objects get two follow hairs per guide
+        a = o.asset
+        guides = a.positions.reshape(a.num_guide_strands, a.verts_per_strand, 4)[:, :, :3].astype(np.float64)
+        o.asset = build_asset(guides, 2, tip_separation=0.5, follow_radius=0.002, rng=rng,
+                              bone_skinning=a.bone_skinning.reshape(-1, 8))
+    assert [o.asset.verts_per_strand for o in sc.objects] == [32, 32, 16, 16, 16, 32]
+    assert [o.asset.follow_per_guide for o in sc.objects] == [0, 0, 2, 2, 0, 0]
+    gpu = BatchedPipeline(ctx, sc)
+    gpu.batch.set_option(gpu.batch.FOLLOW_FORM, form)
+    ora = OraclePipeline(sc)
+    try:
+        for f in range(4):
+            fin = gpu.step(f)
+            ora.step(fin)
+        for i, (h, oh) in enumerate(zip(gpu.hair, ora.hair)):
+            assert_same(h, oh, f"form {form} object {i}")
+    finally:
+        gpu.close()
+
+
 def test_batched_autotune_keeps_state(ctx):
     sc = scene_batched(seed=6, num_objects=4, min_strands=64, max_strands=400, min_tris=800, max_tris=2000,
                        sdf_choices=(24, 32), frames=4)
