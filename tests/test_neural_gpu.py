@@ -173,6 +173,89 @@ def test_collision_through_the_proxy_matches_the_grid(ctx, small_proxy):
         b.close()
 
 
+def _gated_grid_check(ctx, sc, nsdf, frames_before: int):
+    """Runs a proxy frame up to its collision, recomputes the contact band on the host from the
+    network's own outputs (tfx_nsdf_query on the same positions) and returns the proxy path's grid, the
+    full grid of the same pose and the cells the band's lookups read (vertices whose output lies within
+    1e-3 cells of the band's edge are left out, as rounding could put them on either side)."""
+    import torch
+    from tressfx_gb300 import _capi as A
+    from tressfx_gb300.api import SDFCollision
+    from tressfx_gb300.headless import FrameInputs, NeuralPipeline
+    from tressfx_gb300.synthetic import margin_world
+    obj = sc.objects[0]
+    b = NeuralPipeline(ctx, sc, nsdf)
+    cells = int(np.prod(obj.sdf_dims))
+    full = SDFCollision(ctx, cells)
+    full.bind_mesh(b.meshes[0])
+    try:
+        for f in range(frames_before):
+            b.step(f)
+        fin = FrameInputs(sc, frames_before)
+        b.prepare(fin)
+        b.meshes[0].skin(fin.mesh_bones[0])      # NeuralPipeline.run up to the collision
+        b.sim.simulate(b.hair)
+        h, g = b.hair[0], fin.grids[0]
+        pose = sc.meta["pose_fn"](frames_before * sc.dt)
+        P = h.read(A.BUF_POSITIONS).reshape(-1, 4)
+        pos_ptr, _ = h.device_buffer(A.BUF_POSITIONS)
+        out = torch.empty(len(P), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        nsdf.query_device(pos_ptr, len(P), pose, out.data_ptr())
+        torch.cuda.synchronize()
+        y = out.cpu().numpy() / np.float32(nsdf.cell_size)   # the query returns world units, the band is in cells
+        m = margin_world(obj, g)
+        limit = np.float32(np.float32(m) / np.float32(nsdf.cell_size)) + np.float32(2.0)
+        j = np.arange(len(P)) % h.n
+        sure = (j >= 2) & (y < limit - np.float32(1e-3))
+        band = nsdf.collide(h, b.sdfs[0], g, m, pose, band=True)
+        full.update(g)
+        gated, want = b.sdfs[0].read(cells), full.read(cells)
+        o = np.array([g.origin[0], g.origin[1], g.origin[2]], np.float32)
+        q = np.trunc((P[sure, :3].astype(np.float32) - o) / np.float32(g.cell_size)).astype(np.int64)
+        nx, ny, nz = obj.sdf_dims
+        idx = set()
+        for d in np.stack(np.meshgrid(range(3), range(3), range(3), indexing="ij"), -1).reshape(-1, 3):
+            c = q + d
+            ok = (c >= 0).all(1) & (c[:, 0] < nx) & (c[:, 1] < ny) & (c[:, 2] < nz)
+            idx.update(((c[ok, 2] * ny + c[ok, 1]) * nx + c[ok, 0]).tolist())
+        return gated, want, np.array(sorted(idx), np.int64), int(sure.sum()), band
+    finally:
+        full.close()
+        b.close()
+
+
+def test_gated_grid_is_exact_at_the_band_cells(ctx, small_proxy):
+    """The proxy path builds the grid only at the cells its contact band's lookups read; there every
+    word equals the full build's, whatever triangles the coarse 4x4x4-cell map let it skip."""
+    sc, nsdf, _ = small_proxy
+    gated, want, idx, sure, band = _gated_grid_check(ctx, sc, nsdf, 6)
+    assert sure > 0 and band >= sure and len(idx) > 0
+    bad = idx[gated[idx] != want[idx]]
+    assert len(bad) == 0, f"{len(bad)} of {len(idx)} band cells differ"
+
+
+@pytest.fixture(scope="module")
+def grid128_proxy(ctx):
+    """The proxy workload's head mesh (20k triangles) and 128^3 grid, with fewer guides, and a proxy
+    trained briefly (the band is then wider, which the check only welcomes)."""
+    from tressfx_gb300 import synthetic as S
+    from tressfx_gb300.neural import train_proxy
+    sc = S.scene_neural(num_guides=5000, n=32, frames=12)
+    nsdf, rep = train_proxy(ctx, sc.objects[0], poses=64, samples_per_pose=4096, eval_poses=4,
+                            eval_samples_per_pose=4096, steps=1500, batch=4096, lr=3e-3, contact_slack_cells=2.0)
+    yield sc, nsdf, rep
+    nsdf.close()
+
+
+def test_gated_grid_is_exact_at_the_band_cells_128(ctx, grid128_proxy):
+    sc, nsdf, _ = grid128_proxy
+    gated, want, idx, sure, band = _gated_grid_check(ctx, sc, nsdf, 6)
+    assert sure > 0 and band >= sure and len(idx) > 0
+    bad = idx[gated[idx] != want[idx]]
+    assert len(bad) == 0, f"{len(bad)} of {len(idx)} band cells differ"
+
+
 def test_pose_outside_training_range_takes_the_grid_path(ctx, small_proxy):
     """A pose outside the range the proxy was trained on: every vertex is collided on the full grid,
     so the frames equal the grid-collided ones bit for bit and the band reports every vertex."""

@@ -790,36 +790,79 @@ __global__ void __launch_bounds__(QUERY_WARPS * 32) k_nsdf_classify(CollideArgs 
     }
 }
 
-__global__ void __launch_bounds__(256) k_gated_init(uint32_t* __restrict__ w, long long cells, const int* __restrict__ count) {
+// Words of the per-cell marks (the coarse map of 4x4x4-cell blocks follows them).
+__host__ __device__ __forceinline__ long long mark_words(long long cells) { return (cells + 31) / 32; }
+__host__ __device__ __forceinline__ int coarse_dim(int n) { return (n + 3) >> 2; }
+
+// The words' initial value, and the coarse map: the block of every marked cell.
+__global__ void __launch_bounds__(256) k_gated_init(uint32_t* __restrict__ w, const uint32_t* __restrict__ marks,
+                                                    uint32_t* __restrict__ coarse, SdfGrid g, const int* __restrict__ count) {
     if (*count == 0) return;
     const uint32_t v = float_flip3(1e10f);
-    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < cells; c += (long long)gridDim.x * blockDim.x)
+    const long long cells = (long long)g.nx * g.ny * g.nz;
+    const int cbx = coarse_dim(g.nx), cby = coarse_dim(g.ny);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < cells; c += (long long)gridDim.x * blockDim.x) {
         w[c] = v;
+        if ((__ldg(marks + (c >> 5)) >> (c & 31)) & 1u) {
+            const long long nxy = (long long)g.nx * g.ny;
+            const int z = (int)(c / nxy);
+            const long long r = c - (long long)z * nxy;
+            const int y = (int)(r / g.nx), x = (int)(r - (long long)y * g.nx);
+            const int b = ((z >> 2) * cby + (y >> 2)) * cbx + (x >> 2);
+            atomicOr(coarse + (b >> 5), 1u << (b & 31));
+        }
+    }
 }
 
 // ConstructSignedDistanceField (TressFXSDFCollision.hlsl:329-397) restricted to marked cells: every
-// (triangle, cell) pair of a marked cell is evaluated, so each marked cell gets its exact value.
+// (triangle, cell) pair of a marked cell is evaluated, so each marked cell gets its exact value.  A
+// warp takes a triangle, its lanes test the 4x4x4-cell blocks the reference's cell box overlaps, and a
+// triangle whose box holds no marked cell is left at once (it contributes to no marked cell).  Box
+// coordinates use the float reciprocal only below 2^22 cells, where it gives the integer quotient
+// (as in the full construct).
 __global__ void __launch_bounds__(256) k_gated_construct(CollideArgs a) {
     if (*a.bandCount == 0) return;
     const SdfGrid g = a.grid;
     const int lane = threadIdx.x & 31;
     const int warpsTotal = gridDim.x * (blockDim.x >> 5);
+    const long long cells = (long long)g.nx * g.ny * g.nz;
+    const uint32_t* coarse = a.marks + mark_words(cells);
+    const int cbx = coarse_dim(g.nx), cby = coarse_dim(g.ny);
     for (int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < a.ntri; t += warpsTotal) {
         const float3 x0 = xyz(__ldg(a.mesh + 2 * (size_t)__ldg(a.indices + 3 * t + 0)));
         const float3 x1 = xyz(__ldg(a.mesh + 2 * (size_t)__ldg(a.indices + 3 * t + 1)));
         const float3 x2 = xyz(__ldg(a.mesh + 2 * (size_t)__ldg(a.indices + 3 * t + 2)));
         int3 lo, hi;
         tri_cell_box(g, x0, x1, x2, lo, hi);
+        const int bx0 = lo.x >> 2, by0 = lo.y >> 2, bz0 = lo.z >> 2;
+        const int nbx = (hi.x >> 2) - bx0 + 1, nby = (hi.y >> 2) - by0 + 1, nbz = (hi.z >> 2) - bz0 + 1;
+        const int nb = nbx * nby * nbz;
+        bool any = false;
+        for (int k = lane; k < nb && !any; k += 32) {
+            const int kz = k / (nbx * nby), kr = k - kz * nbx * nby, ky = kr / nbx, kx = kr - ky * nbx;
+            const int b = ((bz0 + kz) * cby + (by0 + ky)) * cbx + (bx0 + kx);
+            any = (__ldg(coarse + (b >> 5)) >> (b & 31)) & 1u;
+        }
+        if (!__any_sync(0xffffffffu, any)) continue;
         const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
         const int nxy = nx * ny, vol = nxy * nz;
-        bool prepared = false;
-        TriPre P;
+        const bool floatIdx = vol < (1 << 22);
+        const float inxy = 1.0f / (float)nxy, inx = 1.0f / (float)nx;
+        const TriPre P = tri_pre(x0, x1, x2);
         for (int c = lane; c < vol; c += 32) {
-            const int cz = c / nxy, r = c - cz * nxy, cy = r / nx;
+            int cz, r, cy;
+            if (floatIdx) {
+                cz = (int)(((float)c + 0.5f) * inxy);
+                r = c - cz * nxy;
+                cy = (int)(((float)r + 0.5f) * inx);
+            } else {
+                cz = c / nxy;
+                r = c - cz * nxy;
+                cy = r / nx;
+            }
             const int x = lo.x + (r - cy * nx), y = lo.y + cy, z = lo.z + cz;
             const long long cell = ((long long)z * g.ny + y) * g.nx + x;
             if (!((__ldg(a.marks + (cell >> 5)) >> (cell & 31)) & 1u)) continue;
-            if (!prepared) { P = tri_pre(x0, x1, x2); prepared = true; }
             atomicMin(a.words + cell, float_flip3(signed_dist_pre(sdf_cell_pos(g, x, y, z), P)));
         }
     }
@@ -851,7 +894,9 @@ cudaError_t launch_collide(const CollideArgs& a, cudaStream_t s) {
     if (a.vtot <= 0) return cudaSuccess;
     const long long cells = (long long)a.grid.nx * a.grid.ny * a.grid.nz;
     cudaError_t e = cudaMemsetAsync(a.bandCount, 0, sizeof(int), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(a.marks, 0, sizeof(uint32_t) * (size_t)((cells + 31) / 32), s);
+    const long long coarseBits = (long long)coarse_dim(a.grid.nx) * coarse_dim(a.grid.ny) * coarse_dim(a.grid.nz);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(a.marks, 0, sizeof(uint32_t) * (size_t)(mark_words(cells) + (coarseBits + 31) / 32), s);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_nsdf_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)QUERY_SMEM);
     if (e != cudaSuccess) return e;
     if (a.wtc) {   // the network on the tcgen05 path
@@ -867,7 +912,7 @@ cudaError_t launch_collide(const CollideArgs& a, cudaStream_t s) {
         k_nsdf_classify<<<blocks, QUERY_WARPS * 32, QUERY_SMEM, s>>>(a);
     }
     const unsigned gc = (unsigned)std::min<long long>((cells + 255) / 256, (long long)sm_count() * 16);
-    k_gated_init<<<gc, 256, 0, s>>>(a.words, cells, a.bandCount);
+    k_gated_init<<<gc, 256, 0, s>>>(a.words, a.marks, a.marks + mark_words(cells), a.grid, a.bandCount);
     if (a.ntri > 0) k_gated_construct<<<(unsigned)std::min(( a.ntri + 7) / 8, sm_count() * 32), 256, 0, s>>>(a);
     k_gated_finalize<<<gc, 256, 0, s>>>(a.words, cells, a.bandCount);
     k_band_collide<<<sm_count() * 4, 256, 0, s>>>(a);

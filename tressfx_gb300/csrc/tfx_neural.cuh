@@ -151,7 +151,7 @@ struct CollideArgs {
     float margin;            // world units
     float slackCells;        // band: network distance below margin + slackCells cells
     uint32_t* words;         // the SDF words (FloatFlip3 while built, floats after)
-    uint32_t* marks;         // one bit per grid cell
+    uint32_t* marks;         // one bit per grid cell, then one bit per 4x4x4-cell block (any cell marked)
     int* bandList;           // vertex indices
     int* bandCount;
     const float4* mesh;      // skinned {pos, normal}

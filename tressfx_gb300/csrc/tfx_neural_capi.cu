@@ -285,7 +285,12 @@ extern "C" int tfx_nsdf_collide(tfx_nsdf h, tfx_hair hair, tfx_sdf sdf, const tf
         }
         return TFX_OK;
     }
-    if (int r = nsdf_grow((void**)&h->marks, &h->marksCap, (cells + 31) / 32, sizeof(uint32_t), "tfx_nsdf_collide: marks")) return r;
+    // per-cell marks, then one bit per 4x4x4-cell block
+    const long long coarseBits = (long long)((grid->num_cells_x + 3) / 4) * ((grid->num_cells_y + 3) / 4) *
+                                 ((grid->num_cells_z + 3) / 4);
+    if (int r = nsdf_grow((void**)&h->marks, &h->marksCap, (cells + 31) / 32 + (coarseBits + 31) / 32, sizeof(uint32_t),
+                          "tfx_nsdf_collide: marks"))
+        return r;
     if (int r = nsdf_grow((void**)&h->band_, &h->bandCap, hair->Vtot + 1, sizeof(int), "tfx_nsdf_collide: band")) return r;
     nsdf::CollideArgs a{};
     a.wbf = h->wbf; a.bias = h->bias; a.fr = h->fr; a.pose = pose_of(pose);
