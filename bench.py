@@ -298,26 +298,27 @@ def recorded_frame_ms(ctx, issue_frame, prepare, reps: int) -> float:
     makes) and replayed `reps` times back to back, timed with CUDA events on that stream.  Every replay
     repeats the recorded frame's inputs."""
     import torch
-    ext = torch.cuda.ExternalStream(ctx.stream)
-    g = torch.cuda.CUDAGraph()
-    prepare()
-    ctx.synchronize()
-    with torch.cuda.stream(ext):
-        g.capture_begin(capture_error_mode="relaxed")
-        issue_frame()
-        g.capture_end()
-        for _ in range(3):
-            g.replay()
-    ctx.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(ext):
-        e0.record()
-        for _ in range(reps):
-            g.replay()
-        e1.record()
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    del g
+    with torch.cuda.device(ctx.device):
+        ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", ctx.device))
+        g = torch.cuda.CUDAGraph()
+        prepare()
+        ctx.synchronize()
+        with torch.cuda.stream(ext):
+            g.capture_begin(capture_error_mode="relaxed")
+            issue_frame()
+            g.capture_end()
+            for _ in range(3):
+                g.replay()
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            e0.record()
+            for _ in range(reps):
+                g.replay()
+            e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        del g
     return ms
 
 
